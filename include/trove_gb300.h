@@ -1,0 +1,125 @@
+/*
+ * trove_gb300 — C ABI of the GB300 AoS load/store library.
+ *
+ * The reference (bryancatanzaro/trove) is a header-only device library with
+ * no host API: users write kernels that call load_warp_contiguous /
+ * store_warp_contiguous, the block interface or coalesced_ptr, and launch
+ * them themselves (the reference's tests/benchmark.cu:52-128 and
+ * tests/block.cu:13-54 are exactly such kernels).  This header is the host
+ * boundary that replaces those hand-written kernels: each entry point
+ * launches a kernel built on this library's own implementation of that
+ * device API (include/trove/*.h, same names and signatures as the
+ * reference), on one GPU, stream-ordered and asynchronous.
+ *
+ * Conventions
+ *  - Every function returns a trv_status (0 == TRV_OK); nothing throws.
+ *  - Pointers are device pointers owned by the caller unless a name says
+ *    _host.  `stream` is a cudaStream_t passed as void* (NULL = legacy
+ *    default stream).  Sizes are 64-bit: n counts structs, width is
+ *    sizeof(T) in bytes.
+ *  - Work is enqueued on `stream`; the call returns before it finishes.
+ *    Argument errors are reported synchronously; a launch failure returns
+ *    TRV_ERR_CUDA with the CUDA error available from trv_last_cuda_error().
+ *  - Results are bit-exact copies of the source bytes.
+ *  - Indices are int32.  Gather/scatter skip an index outside [0, bound):
+ *    that output struct (gather) or that source struct (scatter) is left
+ *    untouched, so a bad index never faults the GPU.
+ */
+#ifndef TROVE_GB300_H
+#define TROVE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum trv_status {
+    TRV_OK = 0,
+    TRV_ERR_INVALID_ARGUMENT = 1, /* null pointer with n > 0, width 0, size overflow */
+    TRV_ERR_UNSUPPORTED = 2,      /* path/width combination not offered */
+    TRV_ERR_MISALIGNED = 3,       /* explicit path needs an alignment the pointers lack */
+    TRV_ERR_CUDA = 4,             /* a CUDA call failed; see trv_last_cuda_error() */
+    TRV_ERR_OUT_OF_MEMORY = 5,
+    TRV_ERR_BUDGET = 6,           /* request larger than the configured HBM budget */
+    TRV_ERR_TIMEOUT = 7,
+    TRV_ERR_NOT_FOUND = 8,
+    TRV_ERR_BUSY = 9,
+    TRV_ERR_CANCELLED = 10,
+    TRV_ERR_DEVICE_FLAG = 11      /* a kernel reported an error flag */
+} trv_status;
+
+/* Data-movement strategy.  AUTO picks per (op, width, length, alignment). */
+typedef enum trv_path {
+    TRV_PATH_AUTO = 0,
+    TRV_PATH_WARP = 1,    /* load/store_warp_contiguous: coalesced rounds + register transpose */
+    TRV_PATH_BLOCK = 2,   /* block interface: *_array_warp_contiguous, load/store_array fallback */
+    TRV_PATH_VECTOR = 3,  /* flat copy with the widest vector both pointers allow */
+    TRV_PATH_BULK = 4,    /* TMA bulk copy (cp.async.bulk) staged through shared memory */
+    TRV_PATH_DIRECT = 5,  /* compiler-generated per-thread struct access (baseline) */
+    TRV_PATH_COALESCED = 6 /* coalesced_ptr: contiguity check, warp path or per-thread words */
+} trv_path;
+
+/* Optional launch shape; zero fields mean "choose". */
+typedef struct trv_launch {
+    int32_t path;          /* trv_path */
+    int32_t unroll;        /* structs per thread per pass: 1, 2, 4 or 8 */
+    int32_t block_threads; /* multiple of 32, <= 1024 */
+    int32_t grid_blocks;   /* 0: enough persistent blocks to fill the GPU */
+} trv_launch;
+
+const char* trv_status_string(int32_t status);
+int32_t trv_version(void);
+/* Last CUDA error code seen by this thread's calls (0 if none). */
+int32_t trv_last_cuda_error(void);
+
+/* dst[i] = src[i] for i < n structs of `width` bytes.
+ * Replaces the user kernel `T v = load_warp_contiguous(src + i);
+ * store_warp_contiguous(v, dst + i);` (reference trove/aos.h:66-105,
+ * pattern of tests/benchmark.cu:52-88). */
+int32_t trv_copy(void* dst, const void* src, uint64_t n, uint32_t width, void* stream);
+int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width,
+                    const trv_launch* cfg, void* stream);
+
+/* Copy with a data-dependent early exit: struct i is copied unless its first
+ * 32-bit word w satisfies w % modulus == modulus - 1 (modulus 0: never).
+ * Lanes that exit leave their warp non-converged, so the remaining lanes take
+ * the per-thread fallback.  path is TRV_PATH_WARP (warp_converged() ?
+ * load/store_warp_contiguous : per-thread) or TRV_PATH_BLOCK (the block
+ * interface with its load_array/store_array fallback, reference
+ * trove/block.h:35-65 and tests/block.cu:34-54).  width % 4 == 0, <= 64. */
+int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus,
+                      int32_t path, void* stream);
+
+/* dst[i] = src[idx[i]] for i < n; idx[i] outside [0, src_n) is skipped.
+ * Replaces the coalesced_ptr gather kernel (reference trove/ptr.h:76-90,
+ * tests/benchmark.cu:90-99). */
+int32_t trv_gather(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n,
+                   uint32_t width, void* stream);
+int32_t trv_gather_ex(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n,
+                      uint32_t width, const trv_launch* cfg, void* stream);
+
+/* dst[idx[i]] = src[i] for i < n; idx[i] outside [0, dst_n) is skipped.
+ * With repeated indices the surviving write is unspecified (as in the
+ * reference).  Replaces tests/benchmark.cu:101-110. */
+int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n,
+                    uint32_t width, void* stream);
+int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n,
+                       uint32_t width, const trv_launch* cfg, void* stream);
+
+/* Synthetic inputs: dst[k] = word k of the seeded splitmix64 stream (the same
+ * stream the CPU oracle generates).  No reference counterpart. */
+int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void* stream);
+
+/* Host-buffer copy: src_host -> device staging -> copy kernel -> dst_host,
+ * chunked and overlapped on internal streams; returns when dst_host holds
+ * the result.  Buffers should be pinned for full speed.  No reference
+ * counterpart (the reference has no host API). */
+int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t n, uint32_t width);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TROVE_GB300_H */

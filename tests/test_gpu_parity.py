@@ -1,0 +1,208 @@
+"""GPU parity: every C ABI path against the CPU oracle, bit-exact, through
+the C ABI.  Sizes are small enough for the oracle to finish in seconds; the
+full-size workloads are checked through size-independent properties in
+test_gpu_fullsize.py."""
+import numpy as np
+import pytest
+
+import oracle
+import trove_gb300 as tg
+
+pytestmark = pytest.mark.gpu
+
+WIDTHS = list(range(4, 65, 4))
+SENTINEL = 0xA5
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).cuda()
+
+
+def to_host(t):
+    return t.cpu().numpy()
+
+
+def guarded(torch, nbytes, offset=0, guard=256):
+    """Device byte buffer with sentinel guard bands; returns (buffer, view
+    start) so writes outside [start, start + nbytes) can be detected."""
+    buf = torch.full((guard + offset + nbytes + guard,), SENTINEL, dtype=torch.uint8, device="cuda")
+    return buf, guard + offset
+
+
+def check_guards(buf, start, nbytes):
+    h = to_host(buf)
+    assert (h[:start] == SENTINEL).all(), "write before the destination"
+    assert (h[start + nbytes:] == SENTINEL).all(), "write past the destination"
+    return h[start:start + nbytes]
+
+
+@pytest.mark.parametrize("width", WIDTHS)
+def test_copy_struct_paths(cuda, width):
+    torch = cuda
+    for n in [1, 31, 33, 4097, 65539]:
+        src_h = oracle.random_structs(n, width, seed=width * 1000 + n)
+        src = to_dev(torch, src_h)
+        expect = oracle.copy(src_h, n, width)
+        for path in ["warp", "block", "direct", "vector", "auto"]:
+            for unroll in ([1, 2, 4, 8] if path in ("warp", "block", "direct", "vector") else [0]):
+                buf, start = guarded(torch, n * width)
+                tg.copy(buf[start:], src, n, width, path=path, unroll=unroll)
+                got = check_guards(buf, start, n * width)
+                assert np.array_equal(got, expect), (width, n, path, unroll)
+
+
+@pytest.mark.parametrize("offset", [4, 8, 12])
+@pytest.mark.parametrize("width", [8, 12, 16, 24, 32, 48, 64])
+def test_copy_misaligned(cuda, width, offset):
+    """Struct arrays not aligned to their widest word; the flat path with
+    source and destination at different alignments."""
+    torch = cuda
+    n = 3001
+    src_h = oracle.random_structs(n, width, seed=offset * 7 + width)
+    sbuf, sstart = guarded(torch, n * width, offset=offset)
+    sbuf[sstart:sstart + n * width] = to_dev(torch, src_h)
+    for path in ["warp", "block", "vector", "auto"]:
+        dbuf, dstart = guarded(torch, n * width, offset=(offset * 3) % 16)
+        tg.copy(dbuf[dstart:], sbuf[sstart:], n, width, path=path)
+        got = check_guards(dbuf, dstart, n * width)
+        assert np.array_equal(got, src_h.reshape(-1)), (path, width, offset)
+
+
+@pytest.mark.parametrize("nbytes_width", [(1, 1), (3, 7), (5, 3), (100, 13), (7, 132), (1000, 100)])
+def test_copy_odd_widths(cuda, nbytes_width):
+    torch = cuda
+    n, width = nbytes_width
+    src_h = np.frombuffer(oracle.random_words((n * width + 3) // 4, 9).tobytes()[:n * width], np.uint8)
+    src = to_dev(torch, src_h)
+    buf, start = guarded(torch, n * width, offset=1)
+    tg.copy(buf[start:], src, n, width)
+    assert np.array_equal(check_guards(buf, start, n * width), src_h)
+    with pytest.raises(tg.TroveError):
+        tg.copy(buf[start:], src, n, width, path="warp")
+
+
+@pytest.mark.parametrize("path", ["warp", "block"])
+@pytest.mark.parametrize("width", WIDTHS)
+def test_copy_exit(cuda, width, path):
+    torch = cuda
+    for n, modulus in [(20000, 7), (100003, 625), (4096, 0), (77, 3)]:
+        src_h = oracle.random_structs(n, width, seed=width + n + modulus)
+        init = np.full(n * width, SENTINEL, np.uint8)
+        expect, written = oracle.copy_exit(init, src_h, n, width, modulus)
+        src = to_dev(torch, src_h)
+        dst = to_dev(torch, init)
+        tg.copy_exit(dst, src, n, width, modulus, path=path)
+        assert np.array_equal(to_host(dst), expect), (width, n, modulus, path)
+        if modulus == 625:
+            assert 0 < n - written < n // 100
+
+
+def index_sets(n, seed):
+    return {
+        "perm": oracle.permutation(n, seed),
+        "runs": oracle.run_indices(n, seed),
+        "uniform": oracle.uniform_indices(n, n, seed),
+        "identity": np.arange(n, dtype=np.int32),
+    }
+
+
+@pytest.mark.parametrize("width", WIDTHS)
+def test_gather(cuda, width):
+    torch = cuda
+    for n in [33, 5000, 65536 + 17]:
+        src_h = oracle.random_structs(n, width, seed=width * 31 + n)
+        src = to_dev(torch, src_h)
+        init = np.full(n * width, SENTINEL, np.uint8)
+        for name, idx_h in index_sets(n, seed=n + width).items():
+            idx = torch.from_numpy(idx_h).cuda()
+            expect = oracle.gather(init, src_h, idx_h, n, width)
+            for path in ["coalesced", "direct", "auto", "vector"]:
+                for unroll in ([1, 2, 4, 8] if path in ("coalesced", "direct") else [0]):
+                    dst = to_dev(torch, init)
+                    tg.gather(dst, src, n, idx, n, width, path=path, unroll=unroll)
+                    assert np.array_equal(to_host(dst), expect), (width, n, name, path, unroll)
+
+
+@pytest.mark.parametrize("width", [4, 12, 16, 36, 64])
+def test_gather_out_of_range_indices_are_skipped(cuda, width):
+    torch = cuda
+    n = 4099
+    src_h = oracle.random_structs(n, width, seed=5)
+    idx_h = oracle.uniform_indices(n, n, 6)
+    bad = np.arange(n) % 97 == 3
+    idx_h = idx_h.copy()
+    idx_h[bad] = np.where(np.arange(bad.sum()) % 2 == 0, -5, n + 10)
+    init = np.full(n * width, SENTINEL, np.uint8)
+    expect = init.reshape(n, width).copy()
+    expect[~bad] = src_h[idx_h[~bad]]
+    for path in ["coalesced", "direct", "vector"]:
+        dst = to_dev(torch, init)
+        tg.gather(dst, to_dev(torch, src_h), n, torch.from_numpy(idx_h).cuda(), n, width, path=path)
+        assert np.array_equal(to_host(dst), expect.reshape(-1)), path
+
+
+@pytest.mark.parametrize("width", WIDTHS)
+def test_scatter(cuda, width):
+    torch = cuda
+    for n in [33, 5000, 65536 + 17]:
+        src_h = oracle.random_structs(n, width, seed=width * 17 + n)
+        src = to_dev(torch, src_h)
+        init = np.full(n * width, SENTINEL, np.uint8)
+        for name in ["perm", "identity"]:
+            idx_h = index_sets(n, seed=n)[name]
+            idx = torch.from_numpy(idx_h).cuda()
+            expect = oracle.scatter(init, src_h, idx_h, n, width)
+            for path in ["coalesced", "direct", "auto", "vector"]:
+                dst = to_dev(torch, init)
+                tg.scatter(dst, n, src, idx, n, width, path=path)
+                assert np.array_equal(to_host(dst), expect), (width, n, name, path)
+
+
+def test_scatter_out_of_range_indices_are_skipped(cuda):
+    torch = cuda
+    n, width = 2000, 20
+    src_h = oracle.random_structs(n, width, seed=8)
+    idx_h = oracle.permutation(n, 9).copy()
+    idx_h[::13] = -1
+    keep = idx_h >= 0
+    init = np.full(n * width, SENTINEL, np.uint8)
+    expect = init.reshape(n, width).copy()
+    expect[idx_h[keep]] = src_h[keep]
+    dst = to_dev(torch, init)
+    tg.scatter(dst, n, to_dev(torch, src_h), torch.from_numpy(idx_h).cuda(), n, width)
+    assert np.array_equal(to_host(dst), expect.reshape(-1))
+
+
+def test_fill_matches_oracle_stream(cuda):
+    torch = cuda
+    for nwords, seed in [(1, 0), (1000, 0), (1 << 20, 12345)]:
+        t = torch.empty(nwords, dtype=torch.int32, device="cuda")
+        tg.fill_random_u32(t, nwords, seed)
+        assert np.array_equal(to_host(t).view(np.uint32), oracle.random_words(nwords, seed))
+
+
+def test_copy_host(cuda):
+    torch = cuda
+    for n, width, pinned in [(1, 12, False), (100003, 12, True), ((96 << 20) // 28 + 5, 28, True)]:
+        src_h = torch.from_numpy(oracle.random_structs(n, width, seed=n).reshape(-1).copy())
+        if pinned:
+            src_h = src_h.pin_memory()
+        dst_h = torch.zeros_like(src_h)
+        if pinned:
+            dst_h = dst_h.pin_memory()
+        tg.copy_host(dst_h, src_h, n, width)
+        assert torch.equal(dst_h, src_h)
+
+
+def test_config1_contiguous_copy_12B(cuda):
+    """N = 2^20 structs of 3 x uint32 (12 B), words from seed 0, through
+    load/store_warp_contiguous (one launch, 256 threads per block), bit-exact
+    against the CPU host loop."""
+    torch = cuda
+    n, width = 1 << 20, 12
+    src_h = oracle.random_structs(n, width, seed=0)
+    src = to_dev(torch, src_h)
+    dst = torch.zeros_like(src)
+    tg.copy(dst, src, n, width, path="warp")
+    torch.cuda.synchronize()
+    assert np.array_equal(to_host(dst), oracle.copy(src_h, n, width))

@@ -1,0 +1,264 @@
+// C ABI entry points (include/trove_gb300.h): argument checks, path choice
+// and launch shape, then one kernel launch on the caller's stream.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <unordered_map>
+
+#include "flat.h"
+#include "ops.h"
+#include "runtime.h"
+#include "trove_gb300.h"
+
+namespace trv {
+
+thread_local int g_last_cuda_error = 0;
+
+int cuda_fail(cudaError_t e) {
+    g_last_cuda_error = int(e);
+    return TRV_ERR_CUDA;
+}
+
+int check_launch() {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TRV_OK : cuda_fail(e);
+}
+
+DeviceInfo& device_info() {
+    static std::mutex mu;
+    static DeviceInfo infos[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    DeviceInfo& d = infos[dev];
+    if (!d.ready.load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!d.ready.load(std::memory_order_relaxed)) {
+            cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev);
+            if (d.sm_count <= 0) d.sm_count = 1;
+            d.device = dev;
+            d.ready.store(true, std::memory_order_release);
+        }
+    }
+    return d;
+}
+
+int resident_blocks(const void* func, int block) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> cache[64];
+    DeviceInfo& d = device_info();
+    const void* key = func;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache[d.device].find(key);
+        if (it != cache[d.device].end() && block == 256) return it->second;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, block, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int r = per_sm * d.sm_count;
+    if (block == 256) {
+        std::lock_guard<std::mutex> g(mu);
+        cache[d.device][key] = r;
+    }
+    return r;
+}
+
+int grid_for(const void* func, long long work_items, int items_per_block, int block, int requested) {
+    if (requested > 0) return requested;
+    long long need = (work_items + items_per_block - 1) / items_per_block;
+    if (need < 1) need = 1;
+    const int cap = resident_blocks(func, block);
+    return need < cap ? int(need) : cap;
+}
+
+int unroll_slot(int unroll) {
+    switch (unroll) {
+        case 1: return 0;
+        case 2: return 1;
+        case 4: return 2;
+        case 8: return 3;
+    }
+    return -1;
+}
+
+// Heuristic unroll when the caller gives none: about 16 words in flight per
+// lane (tuned by the autotuner when a cache entry exists).
+int default_unroll(unsigned width) {
+    const unsigned words = width / 4;
+    if (words <= 2) return 8;
+    if (words <= 4) return 4;
+    if (words <= 8) return 2;
+    return 1;
+}
+
+}  // namespace trv
+
+using namespace trv;
+
+namespace {
+
+bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+bool size_ok(uint64_t n, uint32_t width) { return width != 0 && n <= (uint64_t(1) << 62) / width; }
+
+bool struct_width(uint32_t width) { return width % 4 == 0 && width >= 4 && width <= 64; }
+
+int copy_flat(void* dst, const void* src, uint64_t nbytes, int unroll, int grid_req, cudaStream_t st) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(src), b = reinterpret_cast<uintptr_t>(dst);
+    int vec = 16;
+    while (vec > 1 && ((a ^ b) & uintptr_t(vec - 1)) != 0) vec >>= 1;
+    long long head = (long long)((vec - (a & uintptr_t(vec - 1))) & uintptr_t(vec - 1));
+    if ((uint64_t)head > nbytes) head = (long long)nbytes;
+    if (unroll <= 0) unroll = 4;
+    if (unroll_slot(unroll) < 0) return TRV_ERR_INVALID_ARGUMENT;
+    const void* func = flat_copy_func(vec, unroll);
+    const long long body = ((long long)nbytes - head) / vec;
+    const int grid = grid_for(func, body, 256 * unroll, 256, grid_req);
+    launch_flat_copy(src, dst, (long long)nbytes, vec, int(head), unroll, grid, st);
+    return check_launch();
+}
+
+int pick_copy_path(const void* dst, const void* src, uint32_t width) {
+    (void)dst;
+    (void)src;
+    (void)width;
+    return TRV_PATH_VECTOR;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* trv_status_string(int32_t status) {
+    switch (status) {
+        case TRV_OK: return "ok";
+        case TRV_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case TRV_ERR_UNSUPPORTED: return "unsupported path/width combination";
+        case TRV_ERR_MISALIGNED: return "pointer alignment not supported by the requested path";
+        case TRV_ERR_CUDA: return "CUDA error";
+        case TRV_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case TRV_ERR_BUDGET: return "request exceeds the HBM budget";
+        case TRV_ERR_TIMEOUT: return "timed out";
+        case TRV_ERR_NOT_FOUND: return "not found";
+        case TRV_ERR_BUSY: return "busy";
+        case TRV_ERR_CANCELLED: return "cancelled";
+        case TRV_ERR_DEVICE_FLAG: return "a kernel reported an error";
+    }
+    return "unknown status";
+}
+
+int32_t trv_version(void) { return 100; }
+
+int32_t trv_last_cuda_error(void) { return g_last_cuda_error; }
+
+int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, const trv_launch* cfg, void* stream) {
+    if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
+    if (n == 0) return TRV_OK;
+    if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int path = cfg ? cfg->path : TRV_PATH_AUTO;
+    const int unroll = cfg ? cfg->unroll : 0;
+    const int grid_req = cfg ? cfg->grid_blocks : 0;
+    if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
+    if (path == TRV_PATH_AUTO) path = pick_copy_path(dst, src, width);
+    if (path == TRV_PATH_VECTOR) return copy_flat(dst, src, n * width, unroll, grid_req, st);
+    if (path != TRV_PATH_WARP && path != TRV_PATH_BLOCK && path != TRV_PATH_DIRECT) return TRV_ERR_UNSUPPORTED;
+    if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
+    if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
+    const int u = unroll > 0 ? unroll : default_unroll(width);
+    const int slot = unroll_slot(u);
+    if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
+    const int api = path == TRV_PATH_WARP ? 0 : path == TRV_PATH_BLOCK ? 1 : 2;
+    const CopyKernel& k = ops_for_words(int(width / 4))->copy[api][slot];
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
+    k.launch(CopyArgs{src, dst, (long long)n, 0u}, grid, 256, st);
+    return check_launch();
+}
+
+int32_t trv_copy(void* dst, const void* src, uint64_t n, uint32_t width, void* stream) {
+    return trv_copy_ex(dst, src, n, width, nullptr, stream);
+}
+
+int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus, int32_t path,
+                      void* stream) {
+    if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
+    if (n == 0) return TRV_OK;
+    if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
+    if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
+    if (path != TRV_PATH_WARP && path != TRV_PATH_BLOCK) return TRV_ERR_UNSUPPORTED;
+    if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
+    const int u = default_unroll(width);
+    const CopyKernel& k = ops_for_words(int(width / 4))->copy_exit[path == TRV_PATH_WARP ? 0 : 1][unroll_slot(u)];
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, 0);
+    k.launch(CopyArgs{src, dst, (long long)n, modulus}, grid, 256, static_cast<cudaStream_t>(stream));
+    return check_launch();
+}
+
+static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound, const int32_t* idx, uint64_t n,
+                        uint32_t width, const trv_launch* cfg, void* stream) {
+    if (!size_ok(n, width) || !size_ok(bound, width)) return TRV_ERR_INVALID_ARGUMENT;
+    if (n == 0) return TRV_OK;
+    if (!dst || !src || !idx) return TRV_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int path = cfg ? cfg->path : TRV_PATH_AUTO;
+    const int grid_req = cfg ? cfg->grid_blocks : 0;
+    if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
+    if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
+    const bool structs = struct_width(width) && aligned(dst, 4) && aligned(src, 4);
+    if (path == TRV_PATH_AUTO) path = structs ? TRV_PATH_COALESCED : TRV_PATH_VECTOR;
+    if (path == TRV_PATH_VECTOR) {  // generic byte-wise form
+        const long long blocks = (long long)((n + 255) / 256);
+        const int cap = device_info().sm_count * 8;
+        const int g = grid_req > 0 ? grid_req : (blocks < cap ? int(blocks) : cap);
+        if (gather)
+            launch_gather_bytes(src, (long long)bound, idx, dst, (long long)n, width, g, st);
+        else
+            launch_scatter_bytes(src, idx, dst, (long long)bound, (long long)n, width, g, st);
+        return check_launch();
+    }
+    if (path != TRV_PATH_COALESCED && path != TRV_PATH_DIRECT) return TRV_ERR_UNSUPPORTED;
+    if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
+    if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
+    const int u = (cfg && cfg->unroll > 0) ? cfg->unroll : default_unroll(width);
+    const int slot = unroll_slot(u);
+    if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
+    const WidthOps* ops = ops_for_words(int(width / 4));
+    const int mode = path == TRV_PATH_COALESCED ? 0 : 1;
+    const IndexKernel& k = gather ? ops->gather[mode][slot] : ops->scatter[mode][slot];
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
+    k.launch(IndexArgs{src, dst, idx, (long long)n, (long long)bound}, grid, 256, st);
+    return check_launch();
+}
+
+int32_t trv_gather_ex(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n, uint32_t width,
+                      const trv_launch* cfg, void* stream) {
+    return index_op(true, dst, src, src_n, idx, n, width, cfg, stream);
+}
+
+int32_t trv_gather(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n, uint32_t width,
+                   void* stream) {
+    return index_op(true, dst, src, src_n, idx, n, width, nullptr, stream);
+}
+
+int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n, uint32_t width,
+                       const trv_launch* cfg, void* stream) {
+    return index_op(false, dst, src, dst_n, idx, n, width, cfg, stream);
+}
+
+int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n, uint32_t width,
+                    void* stream) {
+    return index_op(false, dst, src, dst_n, idx, n, width, nullptr, stream);
+}
+
+int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void* stream) {
+    if (nwords == 0) return TRV_OK;
+    if (!dst || nwords > (uint64_t(1) << 61)) return TRV_ERR_INVALID_ARGUMENT;
+    const int grid = device_info().sm_count * 8;
+    launch_fill_u32(dst, (long long)nwords, seed, grid, static_cast<cudaStream_t>(stream));
+    return check_launch();
+}
+
+}  // extern "C"

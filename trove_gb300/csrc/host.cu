@@ -1,0 +1,91 @@
+// trv_copy_host: the host-buffer form of trv_copy.  The array moves through
+// device staging in chunks on three streams, so the host->device copy of one
+// chunk, the copy kernel of the previous one and the device->host copy of the
+// one before that overlap (the two copy directions use separate engines).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "runtime.h"
+#include "trove_gb300.h"
+
+namespace trv {
+namespace {
+
+constexpr int kStages = 3;
+constexpr uint64_t kChunkBytes = uint64_t(64) << 20;
+
+struct Staging {
+    std::mutex mu;
+    bool ready = false;
+    void* src[kStages] = {};
+    void* dst[kStages] = {};
+    cudaStream_t st[kStages] = {};
+};
+
+Staging& staging_for_device() {
+    static Staging per_device[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return per_device[dev >= 0 && dev < 64 ? dev : 0];
+}
+
+int prepare(Staging& s) {
+    if (s.ready) return TRV_OK;
+    for (int k = 0; k < kStages; ++k) {
+        cudaError_t e = cudaMalloc(&s.src[k], kChunkBytes);
+        if (e == cudaSuccess) e = cudaMalloc(&s.dst[k], kChunkBytes);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s.st[k], cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            for (int j = 0; j <= k; ++j) {
+                if (s.src[j]) cudaFree(s.src[j]);
+                if (s.dst[j]) cudaFree(s.dst[j]);
+                if (s.st[j]) cudaStreamDestroy(s.st[j]);
+                s.src[j] = s.dst[j] = nullptr;
+                s.st[j] = nullptr;
+            }
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation ? TRV_ERR_OUT_OF_MEMORY : cuda_fail(e);
+        }
+    }
+    s.ready = true;
+    return TRV_OK;
+}
+
+}  // namespace
+}  // namespace trv
+
+using namespace trv;
+
+extern "C" int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t n, uint32_t width) {
+    if (width == 0 || n > (uint64_t(1) << 62) / width) return TRV_ERR_INVALID_ARGUMENT;
+    if (n == 0) return TRV_OK;
+    if (!dst_host || !src_host) return TRV_ERR_INVALID_ARGUMENT;
+    Staging& s = staging_for_device();
+    std::lock_guard<std::mutex> guard(s.mu);
+    int rc = prepare(s);
+    if (rc != TRV_OK) return rc;
+    // Whole structs per chunk, so each chunk is a valid trv_copy.
+    uint64_t per_chunk = kChunkBytes / width;
+    if (per_chunk == 0) return TRV_ERR_UNSUPPORTED;  // one struct larger than a chunk
+    const unsigned char* in = static_cast<const unsigned char*>(src_host);
+    unsigned char* out = static_cast<unsigned char*>(dst_host);
+    int k = 0;
+    for (uint64_t first = 0; first < n; first += per_chunk, k = (k + 1) % kStages) {
+        const uint64_t cnt = n - first < per_chunk ? n - first : per_chunk;
+        const uint64_t off = first * width, bytes = cnt * width;
+        cudaStream_t st = s.st[k];
+        cudaError_t e = cudaMemcpyAsync(s.src[k], in + off, bytes, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e);
+        rc = trv_copy(s.dst[k], s.src[k], cnt, width, st);
+        if (rc != TRV_OK) return rc;
+        e = cudaMemcpyAsync(out + off, s.dst[k], bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_fail(e);
+    }
+    for (int j = 0; j < kStages; ++j) {
+        const cudaError_t e = cudaStreamSynchronize(s.st[j]);
+        if (e != cudaSuccess) return cuda_fail(e);
+    }
+    return TRV_OK;
+}

@@ -1,0 +1,222 @@
+// Kernel templates of the C ABI.  Every struct-typed kernel moves
+// trove::array<unsigned, S> (S = width / 4) through this library's device API
+// (include/trove), so the library's host entry points run exactly the code a
+// user kernel written against that API would run.
+//
+// Work decomposition: a warp owns chunks of 32*U consecutive structs and
+// strides over the array by the grid's warp count; within a chunk lane l owns
+// structs base + u*32 + l (u < U).  All U loads of a chunk are issued before
+// its U stores, which keeps U structs per lane in flight (the memory-level
+// parallelism HBM needs: ~5 MB in flight chip-wide at 6.8 TB/s).  The grid is
+// sized to the resident-block count (152 SMs x occupancy), so each warp makes
+// many passes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <trove/aos.h>
+#include <trove/block.h>
+#include <trove/ptr.h>
+
+namespace trv {
+
+template <int S>
+using aos = trove::array<unsigned, S>;
+
+enum Api { API_WARP = 0, API_BLOCK = 1, API_DIRECT = 2 };
+
+template <int S>
+__device__ __forceinline__ bool exits(const aos<S>& v, unsigned modulus) {
+    return modulus != 0u && (v.head % modulus) == modulus - 1u;
+}
+
+// Load/store of struct i when the caller's warp is converged and its lanes
+// address consecutive structs.
+template <int S, int API>
+__device__ __forceinline__ aos<S> load_conv(const aos<S>* src, long long i) {
+    if constexpr (API == API_WARP)
+        return trove::load_warp_contiguous(src + i);
+    else if constexpr (API == API_BLOCK)
+        return trove::load_array_warp_contiguous<S>(reinterpret_cast<const unsigned*>(src), i);
+    else
+        return src[i];
+}
+
+template <int S, int API>
+__device__ __forceinline__ void store_conv(aos<S>* dst, long long i, const aos<S>& v) {
+    if constexpr (API == API_WARP)
+        trove::store_warp_contiguous(v, dst + i);
+    else if constexpr (API == API_BLOCK)
+        trove::store_array_warp_contiguous(reinterpret_cast<unsigned*>(dst), i, v);
+    else
+        dst[i] = v;
+}
+
+// The same when the warp is not converged.
+template <int S, int API>
+__device__ __forceinline__ aos<S> load_div(const aos<S>* src, long long i) {
+    if constexpr (API == API_BLOCK)
+        return trove::load_array<S>(reinterpret_cast<const unsigned*>(src), i);
+    else if constexpr (API == API_WARP)
+        return trove::detail::divergent_load(src + i);
+    else
+        return src[i];
+}
+
+template <int S, int API>
+__device__ __forceinline__ void store_div(aos<S>* dst, long long i, const aos<S>& v) {
+    if constexpr (API == API_BLOCK)
+        trove::store_array(reinterpret_cast<unsigned*>(dst), i, v);
+    else if constexpr (API == API_WARP)
+        trove::detail::divergent_store(v, dst + i);
+    else
+        dst[i] = v;
+}
+
+template <int S, int API>
+__device__ __forceinline__ aos<S> load_any(const aos<S>* src, long long i) {
+    if constexpr (API == API_DIRECT) return src[i];
+    if (trove::warp_converged()) return load_conv<S, API>(src, i);
+    return load_div<S, API>(src, i);
+}
+
+template <int S, int API>
+__device__ __forceinline__ void store_any(aos<S>* dst, long long i, const aos<S>& v) {
+    if constexpr (API == API_DIRECT) {
+        dst[i] = v;
+    } else {
+        if (trove::warp_converged())
+            store_conv<S, API>(dst, i, v);
+        else
+            store_div<S, API>(dst, i, v);
+    }
+}
+
+struct WarpGrid {
+    int lane;
+    long long warp, warps;
+    __device__ __forceinline__ WarpGrid() {
+        lane = int(threadIdx.x & 31u);
+        warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    }
+};
+
+// dst[i] = src[i], optionally skipping structs whose first word hits the
+// early-exit predicate (EXIT).  Full chunks are warp-uniform, so their loads
+// run with all 32 lanes; stores after an exit see a partial warp and fall back.
+template <int S, int U, int API, bool EXIT>
+__global__ void __launch_bounds__(256)
+copy_kernel(const aos<S>* __restrict__ src, aos<S>* __restrict__ dst, long long n, unsigned modulus) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        if (base + CH <= n) {
+            aos<S> v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = load_conv<S, API>(src, base + u * 32 + g.lane);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (!EXIT || !exits(v[u], modulus)) {
+                    if constexpr (EXIT)
+                        store_any<S, API>(dst, base + u * 32 + g.lane, v[u]);
+                    else
+                        store_conv<S, API>(dst, base + u * 32 + g.lane, v[u]);
+                }
+            }
+        } else {
+#pragma unroll 1
+            for (int u = 0; u < U; ++u) {
+                const long long i = base + u * 32 + g.lane;
+                if (i < n) {
+                    const aos<S> v = load_any<S, API>(src, i);
+                    if (!EXIT || !exits(v, modulus)) store_any<S, API>(dst, i, v);
+                }
+            }
+        }
+    }
+}
+
+// MODE 0: coalesced_ptr (trove::load / trove::store); MODE 1: compiler
+// direct.  Index loads of a chunk are coalesced; every load of the chunk is
+// issued before its stores.
+enum { MODE_COALESCED = 0, MODE_DIRECT = 1 };
+
+template <int S, int U, int MODE>
+__global__ void __launch_bounds__(256)
+gather_kernel(const aos<S>* __restrict__ src, long long src_n, const int* __restrict__ idx,
+              aos<S>* __restrict__ dst, long long n) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    trove::coalesced_ptr<aos<S> > S_(const_cast<aos<S>*>(src));
+    trove::coalesced_ptr<aos<S> > D_(dst);
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        int id[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            id[u] = i < n ? __ldg(idx + i) : -1;
+        }
+        aos<S> v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (id[u] >= 0 && (long long)id[u] < src_n) {
+                if constexpr (MODE == MODE_COALESCED)
+                    v[u] = S_[id[u]];
+                else
+                    v[u] = src[id[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            if (id[u] >= 0 && (long long)id[u] < src_n) {
+                if constexpr (MODE == MODE_COALESCED)
+                    D_[i] = v[u];
+                else
+                    dst[i] = v[u];
+            }
+        }
+    }
+}
+
+template <int S, int U, int MODE>
+__global__ void __launch_bounds__(256)
+scatter_kernel(const aos<S>* __restrict__ src, const int* __restrict__ idx, aos<S>* __restrict__ dst,
+               long long dst_n, long long n) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    trove::coalesced_ptr<aos<S> > S_(const_cast<aos<S>*>(src));
+    trove::coalesced_ptr<aos<S> > D_(dst);
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        int id[U];
+        aos<S> v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            id[u] = i < n ? __ldg(idx + i) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            if (i < n) {
+                if constexpr (MODE == MODE_COALESCED)
+                    v[u] = S_[i];
+                else
+                    v[u] = src[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (id[u] >= 0 && (long long)id[u] < dst_n) {
+                if constexpr (MODE == MODE_COALESCED)
+                    D_[id[u]] = v[u];
+                else
+                    dst[id[u]] = v[u];
+            }
+        }
+    }
+}
+
+}  // namespace trv

@@ -1,0 +1,88 @@
+// Per-width kernel tables.  width_ops.cu is compiled once per struct width
+// S = 1..16 words (-DTRV_WIDTH=S) and fills one WidthOps; the C ABI looks the
+// table up by width and picks an entry by path and unroll.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace trv {
+
+// Unroll factors offered (structs per lane per pass); index = log2(unroll).
+constexpr int kUnrolls = 4;  // 1, 2, 4, 8
+
+struct CopyArgs {
+    const void* src;
+    void* dst;
+    long long n;
+    unsigned modulus;
+};
+
+struct IndexArgs {
+    const void* src;
+    void* dst;
+    const int* idx;
+    long long n;
+    long long bound;  // src_n for gather, dst_n for scatter
+};
+
+template <typename Args>
+struct Kernel {
+    void (*launch)(const Args&, int grid, int block, cudaStream_t);
+    const void* func;  // for occupancy queries
+};
+
+typedef Kernel<CopyArgs> CopyKernel;
+typedef Kernel<IndexArgs> IndexKernel;
+
+struct WidthOps {
+    CopyKernel copy[3][kUnrolls];       // [API_WARP, API_BLOCK, API_DIRECT][unroll]
+    CopyKernel copy_exit[2][kUnrolls];  // [API_WARP, API_BLOCK][unroll]
+    IndexKernel gather[2][kUnrolls];    // [MODE_COALESCED, MODE_DIRECT][unroll]
+    IndexKernel scatter[2][kUnrolls];
+};
+
+// Defined in width_ops.cu, one specialisation per translation unit.
+template <int S>
+const WidthOps& width_ops();
+
+template <> const WidthOps& width_ops<1>();
+template <> const WidthOps& width_ops<2>();
+template <> const WidthOps& width_ops<3>();
+template <> const WidthOps& width_ops<4>();
+template <> const WidthOps& width_ops<5>();
+template <> const WidthOps& width_ops<6>();
+template <> const WidthOps& width_ops<7>();
+template <> const WidthOps& width_ops<8>();
+template <> const WidthOps& width_ops<9>();
+template <> const WidthOps& width_ops<10>();
+template <> const WidthOps& width_ops<11>();
+template <> const WidthOps& width_ops<12>();
+template <> const WidthOps& width_ops<13>();
+template <> const WidthOps& width_ops<14>();
+template <> const WidthOps& width_ops<15>();
+template <> const WidthOps& width_ops<16>();
+
+// Table for S words per struct (1..16), or nullptr.
+inline const WidthOps* ops_for_words(int S) {
+    switch (S) {
+        case 1: return &width_ops<1>();
+        case 2: return &width_ops<2>();
+        case 3: return &width_ops<3>();
+        case 4: return &width_ops<4>();
+        case 5: return &width_ops<5>();
+        case 6: return &width_ops<6>();
+        case 7: return &width_ops<7>();
+        case 8: return &width_ops<8>();
+        case 9: return &width_ops<9>();
+        case 10: return &width_ops<10>();
+        case 11: return &width_ops<11>();
+        case 12: return &width_ops<12>();
+        case 13: return &width_ops<13>();
+        case 14: return &width_ops<14>();
+        case 15: return &width_ops<15>();
+        case 16: return &width_ops<16>();
+    }
+    return nullptr;
+}
+
+}  // namespace trv

@@ -1,0 +1,36 @@
+// Shared host-side runtime state of the library: per-device properties,
+// launch-shape helpers and the thread-local CUDA error slot.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+namespace trv {
+
+struct DeviceInfo {
+    std::atomic<bool> ready{false};
+    int device = 0;
+    int sm_count = 1;
+};
+
+// Properties of the calling thread's current device (cached).
+DeviceInfo& device_info();
+
+// Resident blocks of `func` at `block` threads across the whole GPU.
+int resident_blocks(const void* func, int block);
+
+// Blocks for work_items items at items_per_block each, capped at the
+// resident-block count (a persistent, grid-stride launch); `requested` > 0
+// overrides.
+int grid_for(const void* func, long long work_items, int items_per_block, int block, int requested);
+
+int unroll_slot(int unroll);
+int default_unroll(unsigned width);
+
+// Records a CUDA error for trv_last_cuda_error() and returns TRV_ERR_CUDA.
+int cuda_fail(cudaError_t e);
+// cudaGetLastError() folded into a trv_status.
+int check_launch();
+
+}  // namespace trv

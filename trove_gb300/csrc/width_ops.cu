@@ -1,0 +1,100 @@
+// Instantiates every struct-typed kernel for one width, TRV_WIDTH words
+// (compiled once per width so the build parallelises across widths).
+#include "kernels.cuh"
+#include "ops.h"
+
+#ifndef TRV_WIDTH
+#error "compile with -DTRV_WIDTH=<words per struct>"
+#endif
+
+namespace trv {
+namespace {
+
+constexpr int S = TRV_WIDTH;
+
+template <int U, int API, bool EXIT>
+void launch_copy(const CopyArgs& a, int grid, int block, cudaStream_t st) {
+    copy_kernel<S, U, API, EXIT><<<grid, block, 0, st>>>(
+        static_cast<const aos<S>*>(a.src), static_cast<aos<S>*>(a.dst), a.n, a.modulus);
+}
+
+template <int U, int MODE>
+void launch_gather(const IndexArgs& a, int grid, int block, cudaStream_t st) {
+    gather_kernel<S, U, MODE><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src), a.bound, a.idx,
+                                                      static_cast<aos<S>*>(a.dst), a.n);
+}
+
+template <int U, int MODE>
+void launch_scatter(const IndexArgs& a, int grid, int block, cudaStream_t st) {
+    scatter_kernel<S, U, MODE><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src), a.idx,
+                                                       static_cast<aos<S>*>(a.dst), a.bound, a.n);
+}
+
+// Unroll actually built for table slot k (1, 2, 4, 8): a lane keeps at most
+// 32 words of payload in flight, so wide structs reuse the largest fitting
+// unroll in the upper slots (bounded registers and build time).
+constexpr int unroll_for(int k) {
+    int u = 1 << k;
+    while (u > 1 && u * S > 32) u >>= 1;
+    return u;
+}
+
+template <int API, bool EXIT, int k>
+CopyKernel copy_entry() {
+    constexpr int U = unroll_for(k);
+    return {&launch_copy<U, API, EXIT>, (const void*)&copy_kernel<S, U, API, EXIT>};
+}
+
+template <int API, bool EXIT>
+void fill_copy(CopyKernel (&row)[kUnrolls]) {
+    row[0] = copy_entry<API, EXIT, 0>();
+    row[1] = copy_entry<API, EXIT, 1>();
+    row[2] = copy_entry<API, EXIT, 2>();
+    row[3] = copy_entry<API, EXIT, 3>();
+}
+
+template <int MODE, int k>
+IndexKernel gather_entry() {
+    constexpr int U = unroll_for(k);
+    return {&launch_gather<U, MODE>, (const void*)&gather_kernel<S, U, MODE>};
+}
+
+template <int MODE, int k>
+IndexKernel scatter_entry() {
+    constexpr int U = unroll_for(k);
+    return {&launch_scatter<U, MODE>, (const void*)&scatter_kernel<S, U, MODE>};
+}
+
+template <int MODE>
+void fill_index(IndexKernel (&g)[kUnrolls], IndexKernel (&s)[kUnrolls]) {
+    g[0] = gather_entry<MODE, 0>();
+    g[1] = gather_entry<MODE, 1>();
+    g[2] = gather_entry<MODE, 2>();
+    g[3] = gather_entry<MODE, 3>();
+    s[0] = scatter_entry<MODE, 0>();
+    s[1] = scatter_entry<MODE, 1>();
+    s[2] = scatter_entry<MODE, 2>();
+    s[3] = scatter_entry<MODE, 3>();
+}
+
+WidthOps make_ops() {
+    WidthOps ops;
+    fill_copy<API_WARP, false>(ops.copy[API_WARP]);
+    fill_copy<API_BLOCK, false>(ops.copy[API_BLOCK]);
+    fill_copy<API_DIRECT, false>(ops.copy[API_DIRECT]);
+    fill_copy<API_WARP, true>(ops.copy_exit[API_WARP]);
+    fill_copy<API_BLOCK, true>(ops.copy_exit[API_BLOCK]);
+    fill_index<MODE_COALESCED>(ops.gather[MODE_COALESCED], ops.scatter[MODE_COALESCED]);
+    fill_index<MODE_DIRECT>(ops.gather[MODE_DIRECT], ops.scatter[MODE_DIRECT]);
+    return ops;
+}
+
+}  // namespace
+
+template <>
+const WidthOps& width_ops<S>() {
+    static const WidthOps ops = make_ops();
+    return ops;
+}
+
+}  // namespace trv
