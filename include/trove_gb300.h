@@ -65,14 +65,20 @@ typedef enum trv_path {
 typedef struct trv_launch {
     int32_t path;          /* trv_path */
     int32_t unroll;        /* structs per thread per pass: 1, 2, 4 or 8 */
-    int32_t block_threads; /* multiple of 32, <= 1024 */
+    int32_t block_threads; /* 256 (the only block size offered; 0 = 256) */
     int32_t grid_blocks;   /* 0: enough persistent blocks to fill the GPU */
+    int32_t chunk_bytes;   /* TRV_PATH_BULK: bytes per shared-memory stage, multiple of 16 */
 } trv_launch;
 
 const char* trv_status_string(int32_t status);
 int32_t trv_version(void);
 /* Last CUDA error code seen by this thread's calls (0 if none). */
 int32_t trv_last_cuda_error(void);
+
+/* Synchronizes `stream`, then reads and clears the current device's error
+ * flag, which a kernel sets when one of its bounded waits gives up (the TMA
+ * bulk path).  TRV_ERR_DEVICE_FLAG if it was set. */
+int32_t trv_check_device(void* stream);
 
 /* dst[i] = src[i] for i < n structs of `width` bytes.
  * Replaces the user kernel `T v = load_warp_contiguous(src + i);

@@ -244,9 +244,17 @@ def reference_emulator() -> Emu | None:
 class Cubin:
     """Loads one of the harness cubins into the current CUDA context."""
 
-    def __init__(self, path: Path):
+    def __init__(self, path: Path, device: int = 0):
         self.cu = ctypes.CDLL("libcuda.so.1")
         self.path = Path(path)
+        self._check(self.cu.cuInit(0), "cuInit")
+        ctx = ctypes.c_void_p()
+        self._check(self.cu.cuCtxGetCurrent(ctypes.byref(ctx)), "cuCtxGetCurrent")
+        if not ctx.value:  # bind the device's primary context (the one the runtime API uses)
+            dev = ctypes.c_int()
+            self._check(self.cu.cuDeviceGet(ctypes.byref(dev), device), "cuDeviceGet")
+            self._check(self.cu.cuDevicePrimaryCtxRetain(ctypes.byref(ctx), dev), "cuDevicePrimaryCtxRetain")
+            self._check(self.cu.cuCtxSetCurrent(ctx), "cuCtxSetCurrent")
         mod = ctypes.c_void_p()
         self._check(self.cu.cuModuleLoad(ctypes.byref(mod), str(self.path).encode()), "cuModuleLoad")
         self.mod = mod

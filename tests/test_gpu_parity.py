@@ -43,12 +43,14 @@ def test_copy_struct_paths(cuda, width):
         src_h = oracle.random_structs(n, width, seed=width * 1000 + n)
         src = to_dev(torch, src_h)
         expect = oracle.copy(src_h, n, width)
-        for path in ["warp", "block", "direct", "vector", "auto"]:
+        for path in ["warp", "block", "direct", "vector", "auto", "bulk"]:
             for unroll in ([1, 2, 4, 8] if path in ("warp", "block", "direct", "vector") else [0]):
-                buf, start = guarded(torch, n * width)
-                tg.copy(buf[start:], src, n, width, path=path, unroll=unroll)
-                got = check_guards(buf, start, n * width)
-                assert np.array_equal(got, expect), (width, n, path, unroll)
+                for chunk in ([0, 4096, 48 << 10] if path == "bulk" else [0]):
+                    buf, start = guarded(torch, n * width)
+                    tg.copy(buf[start:], src, n, width, path=path, unroll=unroll, chunk=chunk)
+                    got = check_guards(buf, start, n * width)
+                    assert np.array_equal(got, expect), (width, n, path, unroll, chunk)
+    tg.check_device()
 
 
 @pytest.mark.parametrize("offset", [4, 8, 12])
@@ -61,11 +63,17 @@ def test_copy_misaligned(cuda, width, offset):
     src_h = oracle.random_structs(n, width, seed=offset * 7 + width)
     sbuf, sstart = guarded(torch, n * width, offset=offset)
     sbuf[sstart:sstart + n * width] = to_dev(torch, src_h)
-    for path in ["warp", "block", "vector", "auto"]:
-        dbuf, dstart = guarded(torch, n * width, offset=(offset * 3) % 16)
-        tg.copy(dbuf[dstart:], sbuf[sstart:], n, width, path=path)
-        got = check_guards(dbuf, dstart, n * width)
-        assert np.array_equal(got, src_h.reshape(-1)), (path, width, offset)
+    for path in ["warp", "block", "vector", "auto", "bulk"]:
+        for doff in [(offset * 3) % 16, offset]:
+            dbuf, dstart = guarded(torch, n * width, offset=doff)
+            if path == "bulk" and doff % 16 != offset % 16:
+                with pytest.raises(tg.TroveError, match="alignment"):
+                    tg.copy(dbuf[dstart:], sbuf[sstart:], n, width, path=path)
+                continue
+            tg.copy(dbuf[dstart:], sbuf[sstart:], n, width, path=path)
+            got = check_guards(dbuf, dstart, n * width)
+            assert np.array_equal(got, src_h.reshape(-1)), (path, width, offset, doff)
+    tg.check_device()
 
 
 @pytest.mark.parametrize("nbytes_width", [(1, 1), (3, 7), (5, 3), (100, 13), (7, 132), (1000, 100)])

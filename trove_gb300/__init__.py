@@ -49,7 +49,8 @@ class TroveError(RuntimeError):
 class Launch(ctypes.Structure):
     """trv_launch: optional path / unroll / block / grid choice (0 = choose)."""
     _fields_ = [("path", ctypes.c_int32), ("unroll", ctypes.c_int32),
-                ("block_threads", ctypes.c_int32), ("grid_blocks", ctypes.c_int32)]
+                ("block_threads", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("chunk_bytes", ctypes.c_int32)]
 
 
 _lib = None
@@ -58,6 +59,7 @@ _SIGNATURES = {
     "trv_status_string": (ctypes.c_char_p, [ctypes.c_int32]),
     "trv_version": (ctypes.c_int32, []),
     "trv_last_cuda_error": (ctypes.c_int32, []),
+    "trv_check_device": (ctypes.c_int32, [ctypes.c_void_p]),
     "trv_copy": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                   ctypes.c_void_p]),
     "trv_copy_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
@@ -139,20 +141,25 @@ def _check(rc: int, where: str):
         raise TroveError(rc, where, detail)
 
 
-def _launch(path, unroll, block, grid):
+def _launch(path, unroll, block, grid, chunk=0):
     if isinstance(path, str):
         path = PATHS[path]
-    if not (path or unroll or block or grid):
+    if not (path or unroll or block or grid or chunk):
         return None
-    return ctypes.byref(Launch(int(path), int(unroll), int(block), int(grid)))
+    return ctypes.byref(Launch(int(path), int(unroll), int(block), int(grid), int(chunk)))
 
 
 def copy(dst, src, n: int, width: int, *, path=PATH_AUTO, unroll: int = 0, block: int = 0, grid: int = 0,
-         stream=None):
+         chunk: int = 0, stream=None):
     """dst[i] = src[i] for n structs of `width` bytes (trv_copy_ex)."""
     lib = load()
-    _check(lib.trv_copy_ex(_addr(dst), _addr(src), n, width, _launch(path, unroll, block, grid),
+    _check(lib.trv_copy_ex(_addr(dst), _addr(src), n, width, _launch(path, unroll, block, grid, chunk),
                            _stream(stream)), "trv_copy")
+
+
+def check_device(stream=None):
+    """Synchronize and raise if a kernel's bounded wait gave up."""
+    _check(load().trv_check_device(_stream(stream)), "trv_check_device")
 
 
 def copy_exit(dst, src, n: int, width: int, modulus: int, *, path=PATH_WARP, stream=None):

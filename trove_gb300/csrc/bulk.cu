@@ -1,0 +1,167 @@
+// TRV_PATH_BULK: long contiguous copies through the TMA bulk-copy engine.
+//
+// One thread per CTA drives a ring of kStages shared-memory buffers:
+//   load chunk c:  cp.async.bulk.shared::cluster.global ... complete_tx on
+//                  the stage's mbarrier;
+//   store chunk c: after the mbarrier phase completes,
+//                  cp.async.bulk.global.shared::cta.bulk_group from the
+//                  stage, one bulk group per chunk;
+//   refill:        once the previous chunk's store has finished reading its
+//                  stage (cp.async.bulk.wait_group.read 1) that stage loads
+//                  chunk c - 1 + kStages.
+// So kStages - 1 loads and up to two stores are in flight per SM with a
+// single issuing thread and no register traffic.  Chunks are dealt to CTAs
+// round-robin.  Both pointers must share their address modulo 16 (the bulk
+// engine's alignment unit); the unaligned head and sub-16-byte tail are
+// copied by CTA 0 with plain loads.
+//
+// Every mbarrier wait is bounded: after kSpinLimit polls the CTA records an
+// error in the library's device flag, drains what it has in flight (again
+// bounded) and returns, so a stuck transfer can never hang the GPU.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bulk.h"
+
+namespace trv {
+namespace {
+
+constexpr int kStages = 4;
+constexpr unsigned kSpinLimit = 1u << 24;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// true once the phase with the given parity has completed; false after the
+// poll budget is spent.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (unsigned i = 0; i < kSpinLimit; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* smem, const void* gmem, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(smem)),
+        "l"(gmem), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void bulk_store(void* gmem, const void* smem, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gmem), "r"(smem_addr(smem)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(32)
+bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, long long nbytes, int head,
+                 int chunk, int* flag) {
+    extern __shared__ __align__(128) unsigned char stage_mem[];
+    __shared__ __align__(8) unsigned long long bar[kStages];
+
+    // plain-load edges: [0, head) and the sub-16-byte tail
+    const long long body = ((nbytes - head) / 16) * 16;
+    if (blockIdx.x == 0) {
+        for (int t = threadIdx.x; t < head; t += blockDim.x) dst[t] = src[t];
+        for (long long t = head + body + threadIdx.x; t < nbytes; t += blockDim.x) dst[t] = src[t];
+    }
+    if (threadIdx.x != 0 || body == 0) return;
+
+    const unsigned char* s = src + head;
+    unsigned char* d = dst + head;
+    const long long nchunks = (body + chunk - 1) / chunk;
+    const long long mine = nchunks > blockIdx.x ? (nchunks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (mine == 0) return;
+
+    for (int k = 0; k < kStages; ++k) mbar_init(&bar[k], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+
+    auto chunk_bytes = [&](long long c) -> unsigned {
+        const long long off = c * chunk;
+        return static_cast<unsigned>(body - off < chunk ? body - off : chunk);
+    };
+    auto issue_load = [&](long long k) {  // k-th chunk of this CTA
+        const long long c = blockIdx.x + k * (long long)gridDim.x;
+        const int st = int(k % kStages);
+        const unsigned bytes = chunk_bytes(c);
+        mbar_expect_tx(&bar[st], bytes);
+        bulk_load(stage_mem + (size_t)st * chunk, s + c * chunk, bytes, &bar[st]);
+    };
+
+    const long long prologue = mine < kStages ? mine : kStages;
+    for (long long k = 0; k < prologue; ++k) issue_load(k);
+    long long issued = prologue;
+
+    bool ok = true;
+    long long k = 0;
+    for (; k < mine; ++k) {
+        const int st = int(k % kStages);
+        if (!mbar_wait(&bar[st], unsigned((k / kStages) & 1))) {
+            ok = false;
+            break;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const long long c = blockIdx.x + k * (long long)gridDim.x;
+        bulk_store(d + c * chunk, stage_mem + (size_t)st * chunk, chunk_bytes(c));
+        if (k >= 1 && issued < mine) {
+            bulk_wait_read_1();  // the previous chunk's store has read its stage
+            issue_load(issued++);
+        }
+    }
+    if (!ok) {
+        atomicExch(flag, 1);
+        // drain loads still in flight (bounded), so no transfer targets this
+        // CTA's shared memory after it exits
+        for (long long j = k + 1; j < issued; ++j) mbar_wait(&bar[j % kStages], unsigned((j / kStages) & 1));
+    }
+    bulk_wait_all();
+}
+
+}  // namespace
+
+bool bulk_copy_supported(const void* src, const void* dst) {
+    return ((reinterpret_cast<uintptr_t>(src) ^ reinterpret_cast<uintptr_t>(dst)) & 15u) == 0;
+}
+
+int bulk_copy_smem_bytes(int chunk) { return kStages * chunk; }
+
+cudaError_t launch_bulk_copy(const void* src, void* dst, long long nbytes, int chunk, int grid, int* flag,
+                             cudaStream_t st) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(src);
+    int head = int((16 - (a & 15u)) & 15u);
+    if (head > nbytes) head = int(nbytes);
+    const int smem = bulk_copy_smem_bytes(chunk);
+    cudaError_t e = cudaFuncSetAttribute(bulk_copy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    bulk_copy_kernel<<<grid, 32, smem, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dst),
+                                             nbytes, head, chunk, flag);
+    return cudaGetLastError();
+}
+
+const void* bulk_copy_func() { return (const void*)&bulk_copy_kernel; }
+
+}  // namespace trv

@@ -7,6 +7,7 @@
 #include <mutex>
 #include <unordered_map>
 
+#include "bulk.h"
 #include "flat.h"
 #include "ops.h"
 #include "runtime.h"
@@ -43,6 +44,26 @@ DeviceInfo& device_info() {
         }
     }
     return d;
+}
+
+int* device_flag() {
+    static std::mutex mu;
+    DeviceInfo& d = device_info();
+    std::lock_guard<std::mutex> g(mu);
+    if (!d.flag) {
+        int* p = nullptr;
+        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(p);
+            return nullptr;
+        }
+        d.flag = p;
+    }
+    return d.flag;
 }
 
 int resident_blocks(const void* func, int block) {
@@ -121,6 +142,19 @@ int copy_flat(void* dst, const void* src, uint64_t nbytes, int unroll, int grid_
     return check_launch();
 }
 
+int copy_bulk(void* dst, const void* src, uint64_t nbytes, int chunk, int grid_req, cudaStream_t st) {
+    if (!bulk_copy_supported(src, dst)) return TRV_ERR_MISALIGNED;
+    if (chunk <= 0) chunk = 32 << 10;
+    if (chunk % 16 != 0 || bulk_copy_smem_bytes(chunk) > (227 << 10)) return TRV_ERR_INVALID_ARGUMENT;
+    int* flag = device_flag();
+    if (!flag) return TRV_ERR_OUT_OF_MEMORY;
+    const long long nchunks = (long long)((nbytes + chunk - 1) / chunk);
+    int grid = grid_req > 0 ? grid_req : device_info().sm_count;
+    if (grid > nchunks) grid = nchunks > 0 ? int(nchunks) : 1;
+    const cudaError_t e = launch_bulk_copy(src, dst, (long long)nbytes, chunk, grid, flag, st);
+    return e == cudaSuccess ? TRV_OK : cuda_fail(e);
+}
+
 int pick_copy_path(const void* dst, const void* src, uint32_t width) {
     (void)dst;
     (void)src;
@@ -154,6 +188,22 @@ int32_t trv_version(void) { return 100; }
 
 int32_t trv_last_cuda_error(void) { return g_last_cuda_error; }
 
+int32_t trv_check_device(void* stream) {
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e);
+    int* flag = device_flag();
+    if (!flag) return TRV_ERR_OUT_OF_MEMORY;
+    int h = 0;
+    e = cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (h != 0) {
+        e = cudaMemset(flag, 0, sizeof(int));
+        if (e != cudaSuccess) return cuda_fail(e);
+        return TRV_ERR_DEVICE_FLAG;
+    }
+    return TRV_OK;
+}
+
 int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, const trv_launch* cfg, void* stream) {
     if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
     if (n == 0) return TRV_OK;
@@ -165,6 +215,7 @@ int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, cons
     if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (path == TRV_PATH_AUTO) path = pick_copy_path(dst, src, width);
     if (path == TRV_PATH_VECTOR) return copy_flat(dst, src, n * width, unroll, grid_req, st);
+    if (path == TRV_PATH_BULK) return copy_bulk(dst, src, n * width, cfg ? cfg->chunk_bytes : 0, grid_req, st);
     if (path != TRV_PATH_WARP && path != TRV_PATH_BLOCK && path != TRV_PATH_DIRECT) return TRV_ERR_UNSUPPORTED;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;

@@ -12,10 +12,15 @@ struct DeviceInfo {
     std::atomic<bool> ready{false};
     int device = 0;
     int sm_count = 1;
+    int* flag = nullptr;  // device int: set by kernels whose bounded waits give up
 };
 
 // Properties of the calling thread's current device (cached).
 DeviceInfo& device_info();
+
+// The current device's error flag (allocated and zeroed on first use), or
+// nullptr if that allocation failed.
+int* device_flag();
 
 // Resident blocks of `func` at `block` threads across the whole GPU.
 int resident_blocks(const void* func, int block);
