@@ -13,11 +13,12 @@
 // time (uniform across the tile, so it costs one branch).  One-word structs
 // and structs of more words than the tile has lanes are read per lane.
 //
-// load(p) / store(v, p) take any pointers: when the whole warp is converged
-// and its pointers are consecutive (one __match_any_sync on p - lane) they
-// take the warp-contiguous path; otherwise every lane moves its own struct
-// with the widest aligned words (sector-minimal per-thread access, no
-// shuffles, no pointer broadcast).
+// load(p) / store(v, p) take any pointers.  On a fully converged warp, one
+// __match_any_sync on p - lane tells whether the pointers are consecutive:
+// if so the warp-contiguous path runs; if not, structs of 2..32 words move as
+// cooperative rounds (each struct read by adjacent lanes in one instruction)
+// plus a transpose, and one-word structs move per lane.  A partial warp moves
+// every struct per lane with the widest aligned words.
 #pragma once
 
 #include <trove/detail/dismember.h>
@@ -122,6 +123,95 @@ TROVE_D void contiguous_store(const T& data, T* dst) {
     }
 }
 
+// Warp-cooperative access to 32 unrelated structs (one pointer per lane),
+// in units of U, m = sizeof(T) / sizeof(U) words per struct.  The 32 structs
+// form a 32 x m block of words in lane order; round k (k < m) has lane l move
+// word q = l + 32k of that block: word q % m of the struct whose pointer lane
+// q / m broadcasts.  Lanes reading the same struct read adjacent words in the
+// same instruction, so every struct costs one sector group per round instead
+// of m separate per-lane accesses; the rounds are the row form of the
+// transposition, which converts them to one struct per lane (and back for
+// stores).
+template <typename U, typename T>
+TROVE_D T gather_rows_load(const T* src) {
+    constexpr int m = aliased_size<T, U>::value;
+    const int lane = int(lane_id());
+    regs<U, m> r;
+#pragma unroll
+    for (int k = 0; k < m; ++k) {
+        const int q = lane + 32 * k;
+        const int j = q / m;
+        const T* pj = shfl_any(src, j, 0xFFFFFFFFu, 32);
+        r.v[k] = reinterpret_cast<const U*>(pj)[q - j * m];
+    }
+    r2c_block(r, thread_tile<32>());
+    return fuse_regs<T>(r);
+}
+
+template <typename U, typename T>
+TROVE_D void scatter_rows_store(const T& data, T* dst) {
+    constexpr int m = aliased_size<T, U>::value;
+    const int lane = int(lane_id());
+    regs<U, m> r = lyse_regs<U>(data);
+    c2r_block(r, thread_tile<32>());
+#pragma unroll
+    for (int k = 0; k < m; ++k) {
+        const int q = lane + 32 * k;
+        const int j = q / m;
+        T* pj = shfl_any(dst, j, 0xFFFFFFFFu, 32);
+        reinterpret_cast<U*>(pj)[q - j * m] = r.v[k];
+    }
+}
+
+// Widest word that divides sizeof(T) and that every lane's pointer is aligned
+// to, as log2 of its size (2, 3 or 4); 0 when some pointer is not 4-byte
+// aligned.  One vote, converged warp only.
+template <typename T>
+TROVE_D int warp_word_log2(const void* p) {
+    typedef typename dismember_type<T>::type Umax;
+    const unsigned a = unsigned(reinterpret_cast<std::uintptr_t>(p));
+    const unsigned any = __reduce_or_sync(0xFFFFFFFFu, a & 15u);
+    if (sizeof(Umax) == 16 && (any & 15u) == 0) return 4;
+    if (sizeof(Umax) >= 8 && (any & 7u) == 0) return 3;
+    return (any & 3u) == 0 ? 2 : 0;
+}
+
+// Converged-warp load of 32 arbitrary structs.  When every pointer is aligned
+// to the struct's widest word U: a one-word struct is one vector access per
+// lane, a 2..32-word struct moves as cooperative rounds of U.  Less aligned
+// pointers use the widest word they allow.
+template <typename T>
+TROVE_D T warp_gather_load(const T* src) {
+    typedef typename dismember_type<T>::type Umax;
+    constexpr int mmax = aliased_size<T, Umax>::value;
+    const int lg = warp_word_log2<T>(src);
+    if (lg == floor_log2(int(sizeof(Umax)))) {
+        if constexpr (mmax == 1) return divergent_load(src);
+        if constexpr (mmax >= 2 && mmax <= 32) return gather_rows_load<Umax>(src);
+    }
+    if constexpr (sizeof(T) % 8 == 0 && sizeof(T) / 8 >= 2 && sizeof(T) / 8 <= 32)
+        if (lg >= 3) return gather_rows_load<int2>(src);
+    if constexpr (sizeof(T) / 4 >= 2 && sizeof(T) / 4 <= 32)
+        if (lg >= 2) return gather_rows_load<int>(src);
+    return divergent_load(src);
+}
+
+template <typename T>
+TROVE_D void warp_scatter_store(const T& data, T* dst) {
+    typedef typename dismember_type<T>::type Umax;
+    constexpr int mmax = aliased_size<T, Umax>::value;
+    const int lg = warp_word_log2<T>(dst);
+    if (lg == floor_log2(int(sizeof(Umax)))) {
+        if constexpr (mmax == 1) return divergent_store(data, dst);
+        if constexpr (mmax >= 2 && mmax <= 32) return scatter_rows_store<Umax>(data, dst);
+    }
+    if constexpr (sizeof(T) % 8 == 0 && sizeof(T) / 8 >= 2 && sizeof(T) / 8 <= 32)
+        if (lg >= 3) return scatter_rows_store<int2>(data, dst);
+    if constexpr (sizeof(T) / 4 >= 2 && sizeof(T) / 4 <= 32)
+        if (lg >= 2) return scatter_rows_store<int>(data, dst);
+    divergent_store(data, dst);
+}
+
 // For a fully converged warp: do lanes 0..31 address consecutive structs in
 // lane order?  Lanes agree on p - lane exactly when they do.
 template <typename T>
@@ -147,8 +237,10 @@ TROVE_D void store_warp_contiguous(const T& data, T* dest) {
 template <typename T>
 TROVE_D T load(const T* src) {
     if constexpr (sizeof(T) % 4 == 0) {
-        if (warp_converged() && detail::warp_consecutive(src))
-            return detail::contiguous_load<WARP_SIZE>(src);
+        if (warp_converged()) {
+            if (detail::warp_consecutive(src)) return detail::contiguous_load<WARP_SIZE>(src);
+            return detail::warp_gather_load(src);
+        }
     }
     return detail::divergent_load(src);
 }
@@ -156,8 +248,11 @@ TROVE_D T load(const T* src) {
 template <typename T>
 TROVE_D void store(const T& data, T* dest) {
     if constexpr (sizeof(T) % 4 == 0) {
-        if (warp_converged() && detail::warp_consecutive(dest)) {
-            detail::contiguous_store<WARP_SIZE>(data, dest);
+        if (warp_converged()) {
+            if (detail::warp_consecutive(dest))
+                detail::contiguous_store<WARP_SIZE>(data, dest);
+            else
+                detail::warp_scatter_store(data, dest);
             return;
         }
     }

@@ -53,7 +53,8 @@ typedef enum trv_status {
 /* Data-movement strategy.  AUTO picks per (op, width, length, alignment). */
 typedef enum trv_path {
     TRV_PATH_AUTO = 0,
-    TRV_PATH_WARP = 1,    /* load/store_warp_contiguous: coalesced rounds + register transpose */
+    TRV_PATH_WARP = 1,    /* copy: load/store_warp_contiguous (coalesced rounds + register transpose);
+                             gather/scatter: warp-cooperative row-form rounds, no transpose */
     TRV_PATH_BLOCK = 2,   /* block interface: *_array_warp_contiguous, load/store_array fallback */
     TRV_PATH_VECTOR = 3,  /* flat copy with the widest vector both pointers allow */
     TRV_PATH_BULK = 4,    /* TMA bulk copy (cp.async.bulk) staged through shared memory */
@@ -66,7 +67,8 @@ typedef struct trv_launch {
     int32_t path;          /* trv_path */
     int32_t unroll;        /* structs per thread per pass: 1, 2, 4 or 8 */
     int32_t block_threads; /* 256 (the only block size offered; 0 = 256) */
-    int32_t grid_blocks;   /* 0: enough persistent blocks to fill the GPU */
+    int32_t grid_blocks;   /* 0: one pass per warp (full grid); -1: persistent grid of
+                              resident blocks; > 0: that many blocks, grid-stride */
     int32_t chunk_bytes;   /* TRV_PATH_BULK: bytes per shared-memory stage, multiple of 16 */
 } trv_launch;
 
@@ -97,6 +99,9 @@ int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width,
  * trove/block.h:35-65 and tests/block.cu:34-54).  width % 4 == 0, <= 64. */
 int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus,
                       int32_t path, void* stream);
+/* Same, with the launch shape given (cfg->path is TRV_PATH_WARP or TRV_PATH_BLOCK). */
+int32_t trv_copy_exit_ex(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus,
+                         const trv_launch* cfg, void* stream);
 
 /* dst[i] = src[idx[i]] for i < n; idx[i] outside [0, src_n) is skipped.
  * Replaces the coalesced_ptr gather kernel (reference trove/ptr.h:76-90,

@@ -2,7 +2,8 @@
 //
 // Runs warp-synchronous device code on the CPU: one std::thread per lane,
 // 32 lanes per warp, and the warp intrinsics (__shfl_sync, __ballot_sync,
-// __all_sync, __any_sync, __match_any_sync, __activemask, __syncwarp) built
+// __all_sync, __any_sync, __match_any_sync, __reduce_or_sync, __activemask,
+// __syncwarp) built
 // on per-member-mask barriers.  It lets the same harness source run against
 // two header trees on a machine without a GPU:
 //   * the reference's trove headers (compiled in place, with the
@@ -130,6 +131,19 @@ inline unsigned __ballot_sync(unsigned mask, int pred) {
     unsigned r = 0;
     for (int l = 0; l < 32; ++l)
         if (((mask >> l) & 1u) && emu::t_warp->slot[l][0]) r |= 1u << l;
+    b.arrive_and_wait();
+    return r;
+}
+
+inline unsigned __reduce_or_sync(unsigned mask, unsigned value) {
+    std::barrier<>& b = emu::deposit(mask, &value, sizeof(value));
+    unsigned r = 0;
+    for (int l = 0; l < 32; ++l) {
+        if (!((mask >> l) & 1u)) continue;
+        unsigned o;
+        std::memcpy(&o, emu::t_warp->slot[l], sizeof(o));
+        r |= o;
+    }
     b.arrive_and_wait();
     return r;
 }

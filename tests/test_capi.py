@@ -61,7 +61,9 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.copy_exit(ok, bad, 5, 12, 625, path="block")) == 3
     assert rc_of(lambda: tg.copy_exit(ok, ok, 5, 12, 625, path="vector")) == 2
     assert rc_of(lambda: tg.gather(ok, ok, 10, bad, 5, 12)) == 3
-    assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="warp")) == 2
+    assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="bulk")) == 2
+    assert rc_of(lambda: tg.scatter(ok, 10, ok, ok, 5, 12, path="block")) == 2
+    assert rc_of(lambda: tg.copy_exit(ok, ok, 5, 12, 625, path="warp", unroll=5)) == 1
     assert rc_of(lambda: tg.copy(ok, ok, 5, 12, block=128)) == 2
     assert rc_of(lambda: tg.fill_random_u32(0, 5, 1)) == 1
     assert rc_of(lambda: tg.copy_host(0, ok, 5, 4)) == 1

@@ -124,8 +124,8 @@ def test_gather(cuda, width):
         for name, idx_h in index_sets(n, seed=n + width).items():
             idx = torch.from_numpy(idx_h).cuda()
             expect = oracle.gather(init, src_h, idx_h, n, width)
-            for path in ["coalesced", "direct", "auto", "vector"]:
-                for unroll in ([1, 2, 4, 8] if path in ("coalesced", "direct") else [0]):
+            for path in ["warp", "coalesced", "direct", "auto", "vector"]:
+                for unroll in ([1, 2, 4, 8] if path in ("warp", "coalesced", "direct") else [0]):
                     dst = to_dev(torch, init)
                     tg.gather(dst, src, n, idx, n, width, path=path, unroll=unroll)
                     assert np.array_equal(to_host(dst), expect), (width, n, name, path, unroll)
@@ -143,7 +143,7 @@ def test_gather_out_of_range_indices_are_skipped(cuda, width):
     init = np.full(n * width, SENTINEL, np.uint8)
     expect = init.reshape(n, width).copy()
     expect[~bad] = src_h[idx_h[~bad]]
-    for path in ["coalesced", "direct", "vector"]:
+    for path in ["warp", "coalesced", "direct", "vector"]:
         dst = to_dev(torch, init)
         tg.gather(dst, to_dev(torch, src_h), n, torch.from_numpy(idx_h).cuda(), n, width, path=path)
         assert np.array_equal(to_host(dst), expect.reshape(-1)), path
@@ -160,10 +160,11 @@ def test_scatter(cuda, width):
             idx_h = index_sets(n, seed=n)[name]
             idx = torch.from_numpy(idx_h).cuda()
             expect = oracle.scatter(init, src_h, idx_h, n, width)
-            for path in ["coalesced", "direct", "auto", "vector"]:
-                dst = to_dev(torch, init)
-                tg.scatter(dst, n, src, idx, n, width, path=path)
-                assert np.array_equal(to_host(dst), expect), (width, n, name, path)
+            for path in ["warp", "coalesced", "direct", "auto", "vector"]:
+                for unroll in ([1, 2, 4, 8] if path in ("warp", "coalesced") else [0]):
+                    dst = to_dev(torch, init)
+                    tg.scatter(dst, n, src, idx, n, width, path=path, unroll=unroll)
+                    assert np.array_equal(to_host(dst), expect), (width, n, name, path, unroll)
 
 
 def test_scatter_out_of_range_indices_are_skipped(cuda):
@@ -176,9 +177,34 @@ def test_scatter_out_of_range_indices_are_skipped(cuda):
     init = np.full(n * width, SENTINEL, np.uint8)
     expect = init.reshape(n, width).copy()
     expect[idx_h[keep]] = src_h[keep]
-    dst = to_dev(torch, init)
-    tg.scatter(dst, n, to_dev(torch, src_h), torch.from_numpy(idx_h).cuda(), n, width)
-    assert np.array_equal(to_host(dst), expect.reshape(-1))
+    for path in ["warp", "coalesced", "direct", "vector"]:
+        dst = to_dev(torch, init)
+        tg.scatter(dst, n, to_dev(torch, src_h), torch.from_numpy(idx_h).cuda(), n, width, path=path)
+        assert np.array_equal(to_host(dst), expect.reshape(-1)), path
+
+
+@pytest.mark.parametrize("width", [8, 12, 16, 24, 32, 48, 64])
+def test_index_ops_misaligned(cuda, width):
+    """Source and destination 4 bytes past a 16-byte boundary: the row-form
+    kernels drop to 4-byte words, the coalesced_ptr kernels to the widest
+    word every pointer allows."""
+    torch = cuda
+    n = 3001
+    src_h = oracle.random_structs(n, width, seed=width)
+    sbuf = torch.zeros(n * width + 64, dtype=torch.uint8, device="cuda")
+    sbuf[4:4 + n * width] = to_dev(torch, src_h)
+    idx_h = oracle.permutation(n, 3)
+    idx = torch.from_numpy(idx_h).cuda()
+    init = np.full(n * width, SENTINEL, np.uint8)
+    g_expect = oracle.gather(init, src_h, idx_h, n, width)
+    s_expect = oracle.scatter(init, src_h, idx_h, n, width)
+    for path in ["warp", "coalesced", "direct", "auto"]:
+        dbuf = torch.full((n * width + 64,), SENTINEL, dtype=torch.uint8, device="cuda")
+        tg.gather(dbuf[4:], sbuf[4:], n, idx, n, width, path=path)
+        assert np.array_equal(to_host(dbuf)[4:4 + n * width], g_expect), ("gather", path)
+        dbuf.fill_(SENTINEL)
+        tg.scatter(dbuf[4:], n, sbuf[4:], idx, n, width, path=path)
+        assert np.array_equal(to_host(dbuf)[4:4 + n * width], s_expect), ("scatter", path)
 
 
 def test_fill_matches_oracle_stream(cuda):

@@ -66,6 +66,8 @@ _SIGNATURES = {
                                      ctypes.POINTER(Launch), ctypes.c_void_p]),
     "trv_copy_exit": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                        ctypes.c_uint32, ctypes.c_int32, ctypes.c_void_p]),
+    "trv_copy_exit_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.POINTER(Launch), ctypes.c_void_p]),
     "trv_gather": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
                                     ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p]),
     "trv_gather_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
@@ -162,11 +164,13 @@ def check_device(stream=None):
     _check(load().trv_check_device(_stream(stream)), "trv_check_device")
 
 
-def copy_exit(dst, src, n: int, width: int, modulus: int, *, path=PATH_WARP, stream=None):
+def copy_exit(dst, src, n: int, width: int, modulus: int, *, path=PATH_WARP, unroll: int = 0, grid: int = 0,
+              stream=None):
     """Copy skipping structs whose first word w has w % modulus == modulus - 1."""
     if isinstance(path, str):
         path = PATHS[path]
-    _check(load().trv_copy_exit(_addr(dst), _addr(src), n, width, modulus, path, _stream(stream)),
+    cfg = Launch(int(path), int(unroll), 0, int(grid), 0)
+    _check(load().trv_copy_exit_ex(_addr(dst), _addr(src), n, width, modulus, ctypes.byref(cfg), _stream(stream)),
            "trv_copy_exit")
 
 

@@ -91,8 +91,11 @@ int grid_for(const void* func, long long work_items, int items_per_block, int bl
     if (requested > 0) return requested;
     long long need = (work_items + items_per_block - 1) / items_per_block;
     if (need < 1) need = 1;
-    const int cap = resident_blocks(func, block);
-    return need < cap ? int(need) : cap;
+    if (requested < 0) {  // persistent: no more blocks than can be resident at once
+        const int cap = resident_blocks(func, block);
+        return need < cap ? int(need) : cap;
+    }
+    return need < 0x7FFFFFFFll ? int(need) : 0x7FFFFFFF;  // one pass per warp
 }
 
 int unroll_slot(int unroll) {
@@ -155,11 +158,11 @@ int copy_bulk(void* dst, const void* src, uint64_t nbytes, int chunk, int grid_r
     return e == cudaSuccess ? TRV_OK : cuda_fail(e);
 }
 
+// Measured on GB300: the TMA bulk engine moves long contiguous runs at the
+// copy roofline; it needs src == dst (mod 16), else the flat vector copy.
 int pick_copy_path(const void* dst, const void* src, uint32_t width) {
-    (void)dst;
-    (void)src;
     (void)width;
-    return TRV_PATH_VECTOR;
+    return bulk_copy_supported(src, dst) ? TRV_PATH_BULK : TRV_PATH_VECTOR;
 }
 
 }  // namespace
@@ -233,19 +236,28 @@ int32_t trv_copy(void* dst, const void* src, uint64_t n, uint32_t width, void* s
     return trv_copy_ex(dst, src, n, width, nullptr, stream);
 }
 
-int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus, int32_t path,
-                      void* stream) {
-    if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
+int32_t trv_copy_exit_ex(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus,
+                         const trv_launch* cfg, void* stream) {
+    if (!size_ok(n, width) || !cfg) return TRV_ERR_INVALID_ARGUMENT;
     if (n == 0) return TRV_OK;
     if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
-    if (path != TRV_PATH_WARP && path != TRV_PATH_BLOCK) return TRV_ERR_UNSUPPORTED;
+    if (cfg->path != TRV_PATH_WARP && cfg->path != TRV_PATH_BLOCK) return TRV_ERR_UNSUPPORTED;
+    if (cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
-    const int u = default_unroll(width);
-    const CopyKernel& k = ops_for_words(int(width / 4))->copy_exit[path == TRV_PATH_WARP ? 0 : 1][unroll_slot(u)];
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, 0);
+    const int u = cfg->unroll > 0 ? cfg->unroll : default_unroll(width);
+    const int slot = unroll_slot(u);
+    if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
+    const CopyKernel& k = ops_for_words(int(width / 4))->copy_exit[cfg->path == TRV_PATH_WARP ? 0 : 1][slot];
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, cfg->grid_blocks);
     k.launch(CopyArgs{src, dst, (long long)n, modulus}, grid, 256, static_cast<cudaStream_t>(stream));
     return check_launch();
+}
+
+int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus, int32_t path,
+                      void* stream) {
+    trv_launch cfg = {path, 0, 0, 0, 0};
+    return trv_copy_exit_ex(dst, src, n, width, modulus, &cfg, stream);
 }
 
 static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound, const int32_t* idx, uint64_t n,
@@ -259,7 +271,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
     if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
     const bool structs = struct_width(width) && aligned(dst, 4) && aligned(src, 4);
-    if (path == TRV_PATH_AUTO) path = structs ? TRV_PATH_COALESCED : TRV_PATH_VECTOR;
+    if (path == TRV_PATH_AUTO) path = structs ? TRV_PATH_WARP : TRV_PATH_VECTOR;
     if (path == TRV_PATH_VECTOR) {  // generic byte-wise form
         const long long blocks = (long long)((n + 255) / 256);
         const int cap = device_info().sm_count * 8;
@@ -270,15 +282,23 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
             launch_scatter_bytes(src, idx, dst, (long long)bound, (long long)n, width, g, st);
         return check_launch();
     }
-    if (path != TRV_PATH_COALESCED && path != TRV_PATH_DIRECT) return TRV_ERR_UNSUPPORTED;
+    if (path != TRV_PATH_COALESCED && path != TRV_PATH_DIRECT && path != TRV_PATH_WARP) return TRV_ERR_UNSUPPORTED;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
     const int u = (cfg && cfg->unroll > 0) ? cfg->unroll : default_unroll(width);
     const int slot = unroll_slot(u);
     if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
     const WidthOps* ops = ops_for_words(int(width / 4));
-    const int mode = path == TRV_PATH_COALESCED ? 0 : 1;
-    const IndexKernel& k = gather ? ops->gather[mode][slot] : ops->scatter[mode][slot];
+    const IndexKernel* kp;
+    if (path == TRV_PATH_WARP) {
+        const uintptr_t wb = uintptr_t(ops->rows_word_bytes);
+        const int var = (aligned(dst, wb) && aligned(src, wb)) ? 0 : 1;
+        kp = gather ? &ops->gather_rows[var][slot] : &ops->scatter_rows[var][slot];
+    } else {
+        const int mode = path == TRV_PATH_COALESCED ? 0 : 1;
+        kp = gather ? &ops->gather[mode][slot] : &ops->scatter[mode][slot];
+    }
+    const IndexKernel& k = *kp;
     const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
     k.launch(IndexArgs{src, dst, idx, (long long)n, (long long)bound}, grid, 256, st);
     return check_launch();

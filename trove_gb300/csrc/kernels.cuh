@@ -7,9 +7,11 @@
 // strides over the array by the grid's warp count; within a chunk lane l owns
 // structs base + u*32 + l (u < U).  All U loads of a chunk are issued before
 // its U stores, which keeps U structs per lane in flight (the memory-level
-// parallelism HBM needs: ~5 MB in flight chip-wide at 6.8 TB/s).  The grid is
-// sized to the resident-block count (152 SMs x occupancy), so each warp makes
-// many passes.
+// parallelism HBM needs: ~5 MB in flight chip-wide at 6.8 TB/s).  By default
+// the grid has one chunk per warp (measured on GB300 a few percent faster
+// than a persistent grid-stride grid: blocks retire in address order, so the
+// DRAM working set moves through memory as one window); a persistent grid is
+// available through trv_launch.grid_blocks.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -214,6 +216,88 @@ scatter_kernel(const aos<S>* __restrict__ src, const int* __restrict__ idx, aos<
                     D_[id[u]] = v[u];
                 else
                     dst[id[u]] = v[u];
+            }
+        }
+    }
+}
+
+// Row-form gather / scatter (TRV_PATH_WARP for index ops).  The C ABI knows
+// both sides of the operation, and one side is contiguous, so no struct ever
+// needs to sit in one lane: the warp moves 32 structs as m = 4S/sizeof(V)
+// rounds of 32 words V.  In round k lane l carries word q = l + 32k of the
+// chunk, i.e. word q % m of struct j = q / m, whose index comes from lane j
+// by one 32-bit shuffle.  Gather: the random side is the load (adjacent lanes
+// read adjacent words of one struct in the same instruction), the store lands
+// at word q of the contiguous destination chunk (fully coalesced).  Scatter is
+// the mirror image.  No transposes, no 64-bit pointer broadcasts.
+template <int S, typename V, int U>
+__global__ void __launch_bounds__(256)
+gather_rows_kernel(const V* __restrict__ src, long long src_n, const int* __restrict__ idx, V* __restrict__ dst,
+                   long long n) {
+    constexpr int m = S * 4 / int(sizeof(V));
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        int id[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            const int v = i < n ? __ldg(idx + i) : -1;
+            id[u] = (v >= 0 && (long long)v < src_n) ? v : -1;
+        }
+        V val[U][m];
+        int from[U][m];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int k = 0; k < m; ++k) {
+                const int q = g.lane + 32 * k;
+                const int j = q / m;
+                from[u][k] = __shfl_sync(0xFFFFFFFFu, id[u], j);
+                if (from[u][k] >= 0) val[u][k] = __ldg(src + (long long)from[u][k] * m + (q - j * m));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int k = 0; k < m; ++k)
+                if (from[u][k] >= 0) dst[(base + u * 32) * m + g.lane + 32 * k] = val[u][k];
+        }
+    }
+}
+
+template <int S, typename V, int U>
+__global__ void __launch_bounds__(256)
+scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* __restrict__ dst, long long dst_n,
+                    long long n) {
+    constexpr int m = S * 4 / int(sizeof(V));
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        int id[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            const int v = i < n ? __ldg(idx + i) : -1;
+            id[u] = (v >= 0 && (long long)v < dst_n) ? v : -1;
+        }
+        V val[U][m];
+        int to[U][m];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int k = 0; k < m; ++k) {
+                const int q = g.lane + 32 * k;
+                to[u][k] = __shfl_sync(0xFFFFFFFFu, id[u], q / m);
+                if (to[u][k] >= 0) val[u][k] = __ldg(src + (base + u * 32) * m + q);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int k = 0; k < m; ++k) {
+                const int q = g.lane + 32 * k;
+                if (to[u][k] >= 0) dst[(long long)to[u][k] * m + (q - (q / m) * m)] = val[u][k];
             }
         }
     }

@@ -39,6 +39,10 @@ struct WidthOps {
     CopyKernel copy_exit[2][kUnrolls];  // [API_WARP, API_BLOCK][unroll]
     IndexKernel gather[2][kUnrolls];    // [MODE_COALESCED, MODE_DIRECT][unroll]
     IndexKernel scatter[2][kUnrolls];
+    // Row-form kernels: [0] the widest word dividing the width, [1] 4-byte words.
+    IndexKernel gather_rows[2][kUnrolls];
+    IndexKernel scatter_rows[2][kUnrolls];
+    int rows_word_bytes;  // size of the word used by slot [0]
 };
 
 // Defined in width_ops.cu, one specialisation per translation unit.

@@ -45,6 +45,50 @@ CopyKernel copy_entry() {
     return {&launch_copy<U, API, EXIT>, (const void*)&copy_kernel<S, U, API, EXIT>};
 }
 
+// Widest word dividing the struct: 16, 8 or 4 bytes.
+constexpr int kWideWord = (S % 4 == 0) ? 16 : (S % 2 == 0) ? 8 : 4;
+template <int B>
+struct word_of;
+template <>
+struct word_of<16> {
+    typedef uint4 type;
+};
+template <>
+struct word_of<8> {
+    typedef uint2 type;
+};
+template <>
+struct word_of<4> {
+    typedef unsigned type;
+};
+
+template <typename V, int U>
+void launch_gather_rows(const IndexArgs& a, int grid, int block, cudaStream_t st) {
+    gather_rows_kernel<S, V, U><<<grid, block, 0, st>>>(static_cast<const V*>(a.src), a.bound, a.idx,
+                                                        static_cast<V*>(a.dst), a.n);
+}
+
+template <typename V, int U>
+void launch_scatter_rows(const IndexArgs& a, int grid, int block, cudaStream_t st) {
+    scatter_rows_kernel<S, V, U><<<grid, block, 0, st>>>(static_cast<const V*>(a.src), a.idx,
+                                                         static_cast<V*>(a.dst), a.bound, a.n);
+}
+
+template <typename V, int k>
+void rows_entries(IndexKernel& g, IndexKernel& s) {
+    constexpr int U = unroll_for(k);
+    g = {&launch_gather_rows<V, U>, (const void*)&gather_rows_kernel<S, V, U>};
+    s = {&launch_scatter_rows<V, U>, (const void*)&scatter_rows_kernel<S, V, U>};
+}
+
+template <typename V>
+void fill_rows(IndexKernel (&g)[kUnrolls], IndexKernel (&s)[kUnrolls]) {
+    rows_entries<V, 0>(g[0], s[0]);
+    rows_entries<V, 1>(g[1], s[1]);
+    rows_entries<V, 2>(g[2], s[2]);
+    rows_entries<V, 3>(g[3], s[3]);
+}
+
 template <int API, bool EXIT>
 void fill_copy(CopyKernel (&row)[kUnrolls]) {
     row[0] = copy_entry<API, EXIT, 0>();
@@ -86,6 +130,9 @@ WidthOps make_ops() {
     fill_copy<API_BLOCK, true>(ops.copy_exit[API_BLOCK]);
     fill_index<MODE_COALESCED>(ops.gather[MODE_COALESCED], ops.scatter[MODE_COALESCED]);
     fill_index<MODE_DIRECT>(ops.gather[MODE_DIRECT], ops.scatter[MODE_DIRECT]);
+    fill_rows<typename word_of<kWideWord>::type>(ops.gather_rows[0], ops.scatter_rows[0]);
+    fill_rows<unsigned>(ops.gather_rows[1], ops.scatter_rows[1]);
+    ops.rows_word_bytes = kWideWord;
     return ops;
 }
 
