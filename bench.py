@@ -1,26 +1,36 @@
 #!/usr/bin/env python3
 """Benchmark of the AoS hot path on one GB300 (replicas when N > 1).
 
-Default workload, the width sweep: for s = 1..16 uint32 words (4..64-byte
-structs), a 2 GiB array of N_s = 2^31 / (4 s) structs of seeded random words
-is copied through this library's device API twice — once with
-load/store_warp_contiguous and once with the block interface
-(load/store_array_warp_contiguous) — and in both kernels a lane exits between
-its load and its store when its struct's first word w has w % 625 == 624, so
-about 5 % of 32-struct warp groups run non-converged and take the per-thread
-fallback.  One step = those 32 launches.  GB/s counts bytes read + bytes
-written (the skipped structs are not written).
+--workload sweep (default; the width sweep): for s = 1..16 uint32 words
+  (4..64-byte structs), a 2 GiB array of N_s = 2^31 / (4 s) structs of seeded
+  random words is copied through this library's device API twice — once with
+  load/store_warp_contiguous, once with the block interface
+  (load/store_array_warp_contiguous) — and in both kernels a lane exits between
+  its load and its store when its struct's first word w has w % 625 == 624, so
+  about 5 % of 32-struct warp groups run non-converged and take the per-thread
+  fallback.  One step = those 32 launches.
+--workload gather: dst[i] = src[idx[i]] over 2^24 structs for widths
+  {8,12,16,24,32,48,64} B and index patterns permutation / runs of 32 /
+  identity; one step = those 21 gathers.
+--workload batch: 4096 arrays, lengths log-uniform in [2^10, 2^22] structs,
+  widths uniform from {4,12,20,36,64} B, 50 % copy / 40 % gather (uniform
+  indices) / 10 % scatter (permutation); one step = the whole batch as one
+  persistent launch replayed from a CUDA graph; the same work as one plain
+  launch per array is timed beside it.
 
-Timed work uses inputs far larger than L2 (2 GiB per array), so no L2 flush
-is needed between iterations.  `e2e` measures the same sweep through the
-host-buffer entry point trv_copy_host (pinned host memory in and out inside
-the timed region).  `--impl reference` times the CPU form of the path (the
-oracle's multithreaded port) on the same metric.
+GB/s counts bytes read + bytes written + index bytes.  Every array is far
+larger than L2 or the step streams far more than L2 (126 MB), so no flush is
+needed between iterations.  Launch shapes come from the library's autotuner,
+run before the timed region (its cache is saved and reloaded).  `e2e` times the
+same work with pinned host buffers in and out inside the timed region.
+`--impl reference` times the CPU form of the path (the oracle's
+multithreaded port) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -38,15 +48,11 @@ ARRAY_BYTES = 1 << 31
 MODULUS = 625
 SENTINEL = 0xA5
 WORDS = list(range(1, 17))
-CONFIG = {
-    "workload": "width sweep: contiguous AoS copy, s=1..16 x uint32 (4-64 B), 2 GiB arrays, "
-                "load/store_warp_contiguous + block interface, 5% warps diverged by early exit",
-    "structs_per_width": {str(s): ARRAY_BYTES // (4 * s) for s in WORDS},
-    "exit_predicate": "first word % 625 == 624",
-    "launches_per_step": 32,
-    "l2": "inputs larger than L2 (2 GiB arrays), no flush",
-    "parallelism": "replicas",
-}
+GATHER_N = 1 << 24
+GATHER_WIDTHS = [8, 12, 16, 24, 32, 48, 64]
+GATHER_PATTERNS = ["perm", "runs", "identity"]
+BATCH_COUNT = 4096
+BATCH_WIDTHS = [4, 12, 20, 36, 64]
 
 
 def parse():
@@ -55,9 +61,13 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["trove", "reference"], default="trove")
+    p.add_argument("--workload", choices=["sweep", "gather", "batch"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-check", action="store_true")
+    p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--tune-cache", default=os.environ.get(
+        "TROVE_GB300_TUNE_CACHE", str(Path.home() / ".cache" / "trove_gb300" / "autotune.json")))
     return p.parse_args()
 
 
@@ -75,6 +85,7 @@ def dist_setup(args):
 
 
 def reduce_max(value: float, world: int, device=None) -> float:
+    """Maximum of `value` over all ranks (the slowest replica's time)."""
     if world <= 1:
         return value
     import torch
@@ -140,54 +151,483 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-# ---- the trove arm -------------------------------------------------------------
+def timed(torch, dev, stream, world, steps, step_fn, label_events=True):
+    """Run `steps` steps between barriers and device syncs; returns (max ms
+    over ranks, per-launch events, clock record)."""
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    clocks = Clocks(dev.index or 0)
+    events = [] if label_events else None
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        step_fn(events)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    clock_info = clocks.stop()
+    barrier(world)
+    return reduce_max(a.elapsed_time(b), world, dev), events, clock_info
 
-def sweep_plan():
-    return [(s, 4 * s, ARRAY_BYTES // (4 * s)) for s in WORDS]
+
+def launch_with_events(torch, stream, events, key, fn):
+    if events is None:
+        fn()
+        return
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    fn()
+    b.record(stream)
+    events.append((key, a, b))
 
 
-def verify_sweep(torch, tg, src, dst, plan):
-    """One untimed pass with dst pre-filled; checks every width and both APIs
-    on the device against an independent torch computation of the expected
-    bytes.  Returns structs written per width."""
-    written = {}
-    for s, w, n in plan:
-        words0 = src[: n * w].view(torch.int32).view(n, s)[:, 0].to(torch.int64) & 0xFFFFFFFF
-        skip = (words0 % MODULUS) == (MODULUS - 1)
-        written[s] = int(n - int(skip.sum()))
-        srcv = src[: n * w].view(n, w)
-        for path in (tg.PATH_WARP, tg.PATH_BLOCK):
-            dst.fill_(SENTINEL)
-            tg.copy_exit(dst, src, n, w, MODULUS, path=path)
-            dv = dst[: n * w].view(n, w)
-            ok = torch.equal(dv[~skip], srcv[~skip]) and bool((dv[skip] == SENTINEL).all())
-            ok = ok and bool((dst[n * w:] == SENTINEL).all())
+def kernel_table(events, bytes_of, peak):
+    per = {}
+    for key, a, b in events:
+        per.setdefault(key, []).append(a.elapsed_time(b))
+    rows = []
+    for key, times in per.items():
+        avg = sum(times) / len(times)
+        alg = bytes_of(key)
+        rows.append({"kernel": key, "launches": len(times), "total_ms": round(sum(times), 3),
+                     "avg_ms": round(avg, 4), "bytes_per_launch": alg, "gbs": round(alg / avg / 1e6, 1),
+                     "frac": round(alg / avg / 1e6 / peak, 4)})
+    rows.sort(key=lambda r: -r["total_ms"])
+    return rows
+
+
+def host_mem_available() -> int:
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def load_tune_cache(tg, path):
+    try:
+        if Path(path).exists():
+            tg.autotune_load(path)
+    except Exception:
+        pass
+
+
+def save_tune_cache(tg, path):
+    try:
+        Path(path).parent.mkdir(parents=True, exist_ok=True)
+        tg.autotune_save(path)
+    except Exception:
+        pass
+
+
+# ---- workloads -------------------------------------------------------------------
+
+class Sweep:
+    name = "width sweep"
+    config = {
+        "workload": "width sweep: contiguous AoS copy, s=1..16 x uint32 (4-64 B), 2 GiB arrays, "
+                    "load/store_warp_contiguous + block interface, 5% warps diverged by early exit",
+        "structs_per_width": {str(s): ARRAY_BYTES // (4 * s) for s in WORDS},
+        "exit_predicate": "first word % 625 == 624",
+        "launches_per_step": 32,
+        "l2": "inputs larger than L2 (2 GiB arrays), no flush",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        self.torch, self.tg, self.dev = torch, tg, dev
+        self.plan = [(s, 4 * s, ARRAY_BYTES // (4 * s)) for s in WORDS]
+        self.src = torch.empty(ARRAY_BYTES + 256, dtype=torch.uint8, device=dev)
+        self.dst = torch.empty_like(self.src)
+        tg.fill_random_u32(self.src, (ARRAY_BYTES + 256) // 4, seed=0)
+        self.written = {s: n for s, _, n in self.plan}
+        self.tuned = {}
+
+    def tune(self):
+        tg = self.tg
+        for s, w, n in self.plan:
+            for op, path in ((tg.OP_COPY_EXIT_WARP, tg.PATH_WARP), (tg.OP_COPY_EXIT_BLOCK, tg.PATH_BLOCK)):
+                if tg.autotune_lookup(tg.SCOPE_CALL, op, w, n) is None:
+                    tg.autotune_call(op, w, n)
+                self.tuned[f"{'warp' if path == tg.PATH_WARP else 'block'}_{w}B"] = \
+                    tg.autotune_lookup(tg.SCOPE_CALL, op, w, n)[0].unroll
+
+    def verify(self):
+        torch, tg = self.torch, self.tg
+        for s, w, n in self.plan:
+            words0 = self.src[: n * w].view(torch.int32).view(n, s)[:, 0].to(torch.int64) & 0xFFFFFFFF
+            skip = (words0 % MODULUS) == (MODULUS - 1)
+            self.written[s] = int(n - int(skip.sum()))
+            srcv = self.src[: n * w].view(n, w)
+            for path in (tg.PATH_WARP, tg.PATH_BLOCK):
+                self.dst.fill_(SENTINEL)
+                tg.copy_exit(self.dst, self.src, n, w, MODULUS, path=path)
+                dv = self.dst[: n * w].view(n, w)
+                ok = torch.equal(dv[~skip], srcv[~skip]) and bool((dv[skip] == SENTINEL).all())
+                ok = ok and bool((self.dst[n * w:] == SENTINEL).all())
+                if not ok:
+                    raise SystemExit(f"bench verification failed: width {w} B, path {path}")
+
+    def bytes_per_step(self):
+        return sum(n * w + self.written[s] * w for s, w, n in self.plan) * 2
+
+    def launches_per_step(self):
+        return 2 * len(self.plan)
+
+    def step(self, stream, events):
+        torch, tg = self.torch, self.tg
+        for s, w, n in self.plan:
+            for path in (tg.PATH_WARP, tg.PATH_BLOCK):
+                key = f"copy_exit_{'warp' if path == tg.PATH_WARP else 'block'}_{w}B"
+                launch_with_events(torch, stream, events, key, lambda: tg.copy_exit(
+                    self.dst, self.src, n, w, MODULUS, path=path, stream=stream))
+
+    def kernel_bytes(self, key):
+        w = int(key.rsplit("_", 1)[1][:-1])
+        s, n = w // 4, ARRAY_BYTES // w
+        return n * w + self.written[s] * w
+
+    def e2e(self, world, steps):
+        torch, tg = self.torch, self.tg
+        h_src = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
+        h_dst = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
+        h_src.copy_(self.src[:ARRAY_BYTES].cpu())
+        tg.copy_host(h_dst, h_src, ARRAY_BYTES // 64, 64)  # warm the staging ring
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for s, w, n in self.plan:
+                tg.copy_host(h_dst, h_src, n, w)
+        el = reduce_max(time.perf_counter() - t0, world, self.dev)
+        if not torch.equal(h_dst, h_src):
+            raise SystemExit("e2e verification failed")
+        io = sum(n * w for s, w, n in self.plan)
+        return {"value": round(steps * 2 * io * world / el / 1e9, 2), "unit": UNIT, "h2d_bytes_per_step": io,
+                "d2h_bytes_per_step": io, "steps": steps,
+                "path": "trv_copy_host per width: pinned host buffers, chunked H2D / copy kernel / D2H overlap"}
+
+    def extra(self):
+        return {"tuned_unroll": self.tuned}
+
+
+class Gather:
+    name = "gather"
+    config = {
+        "workload": "random gather dst[i]=src[idx[i]], 2^24 structs, widths 8-64 B, "
+                    "idx = permutation / runs of 32 (p=0.5) / identity",
+        "structs": GATHER_N, "widths": GATHER_WIDTHS, "patterns": GATHER_PATTERNS,
+        "l2": "each step streams 21 gathers over 0.3-2 GB arrays, no flush",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        import oracle  # index patterns for the workload come from the seeded generators
+        self.torch, self.tg, self.dev = torch, tg, dev
+        n = GATHER_N
+        self.src = torch.empty(n * 64 + 256, dtype=torch.uint8, device=dev)
+        tg.fill_random_u32(self.src, (n * 64 + 256) // 4, seed=0)
+        self.dst = torch.empty(n * 64, dtype=torch.uint8, device=dev)
+        self.idx = {"perm": torch.from_numpy(oracle.permutation(n, 1)).to(dev),
+                    "runs": torch.from_numpy(oracle.run_indices(n, 2)).to(dev),
+                    "identity": torch.arange(n, dtype=torch.int32, device=dev)}
+        self.tuned = {}
+
+    def tune(self):
+        tg = self.tg
+        for w in GATHER_WIDTHS:
+            if tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_GATHER, w, GATHER_N) is None:
+                tg.autotune_call(tg.OP_GATHER, w, GATHER_N)
+            c = tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_GATHER, w, GATHER_N)[0]
+            self.tuned[f"{w}B"] = {"path": c.path, "unroll": c.unroll, "cache_policy": c.cache_policy}
+
+    def verify(self):
+        torch, tg, n = self.torch, self.tg, GATHER_N
+        for w in GATHER_WIDTHS:
+            srcv = self.src[: n * w].view(n, w)
+            for p in GATHER_PATTERNS:
+                tg.gather(self.dst, self.src, n, self.idx[p], n, w)
+                if not torch.equal(self.dst[: n * w].view(n, w), srcv[self.idx[p].long()]):
+                    raise SystemExit(f"bench verification failed: gather {w} B {p}")
+
+    def bytes_per_step(self):
+        return sum((2 * w + 4) * GATHER_N for w in GATHER_WIDTHS) * len(GATHER_PATTERNS)
+
+    def launches_per_step(self):
+        return len(GATHER_WIDTHS) * len(GATHER_PATTERNS)
+
+    def step(self, stream, events):
+        for w in GATHER_WIDTHS:
+            for p in GATHER_PATTERNS:
+                launch_with_events(self.torch, stream, events, f"gather_{p}_{w}B", lambda: self.tg.gather(
+                    self.dst, self.src, GATHER_N, self.idx[p], GATHER_N, w, stream=stream))
+
+    def kernel_bytes(self, key):
+        return (2 * int(key.rsplit("_", 1)[1][:-1]) + 4) * GATHER_N
+
+    def e2e(self, world, steps):
+        """Per gather: H2D of that step's indices and source, gather, D2H of
+        the result, all through pinned host memory."""
+        torch, tg, n = self.torch, self.tg, GATHER_N
+        h_src = torch.empty(n * 64, dtype=torch.uint8).pin_memory()
+        h_src.copy_(self.src[: n * 64].cpu())
+        h_idx = {p: self.idx[p].cpu().pin_memory() for p in GATHER_PATTERNS}
+        h_dst = torch.empty(n * 64, dtype=torch.uint8).pin_memory()
+        d_idx = torch.empty(n, dtype=torch.int32, device=self.dev)
+        stream = torch.cuda.current_stream(self.dev)
+        barrier(world)
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        for _ in range(steps):
+            for w in GATHER_WIDTHS:
+                for p in GATHER_PATTERNS:
+                    self.src[: n * w].copy_(h_src[: n * w], non_blocking=True)
+                    d_idx.copy_(h_idx[p], non_blocking=True)
+                    tg.gather(self.dst, self.src, n, d_idx, n, w, stream=stream)
+                    h_dst[: n * w].copy_(self.dst[: n * w], non_blocking=True)
+                    h2d += n * w + 4 * n
+                    d2h += n * w
+        torch.cuda.synchronize(self.dev)
+        el = reduce_max(time.perf_counter() - t0, world, self.dev)
+        return {"value": round(steps * self.bytes_per_step() * world / el / 1e9, 2), "unit": UNIT,
+                "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps, "steps": steps,
+                "path": "per gather: pinned H2D of src + idx, trv_gather, pinned D2H of dst"}
+
+    def extra(self):
+        return {"tuned": self.tuned}
+
+
+class Batch:
+    name = "batch"
+    config = {
+        "workload": "4096 AoS arrays in one persistent launch (CUDA graph): len log-uniform [2^10, 2^22] "
+                    "structs, width uniform {4,12,20,36,64} B, 50% copy / 40% gather (uniform idx) / "
+                    "10% scatter (permutation); compared with one plain launch per array",
+        "arrays": BATCH_COUNT, "widths": BATCH_WIDTHS, "seed": 4,
+        "l2": "each step moves ~110 GB, no flush",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        import numpy as np
+        self.torch, self.tg, self.dev = torch, tg, dev
+        rng = np.random.default_rng(4)
+        ops = rng.choice([0, 1, 2], size=BATCH_COUNT, p=[0.5, 0.4, 0.1])
+        widths = rng.choice(BATCH_WIDTHS, size=BATCH_COUNT)
+        lens = np.exp(rng.uniform(math.log(1 << 10), math.log(1 << 22), size=BATCH_COUNT)).astype(np.int64)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(4)
+        self.tasks, self.keep = [], []
+        for k in range(BATCH_COUNT):
+            op, w, n = int(ops[k]), int(widths[k]), int(lens[k])
+            src = torch.empty(n * w, dtype=torch.uint8, device=dev)
+            tg.fill_random_u32(src, n * w // 4, seed=100 + k)
+            dst = torch.empty_like(src)
+            idx = None
+            if op == 1:
+                idx = torch.empty(n, dtype=torch.int32, device=dev)
+                tg.fill_uniform_indices(idx, n, n, seed=200 + k)
+            elif op == 2:
+                idx = torch.randperm(n, generator=gen, device=dev, dtype=torch.int32)
+            self.tasks.append(dict(op=op, width=w, n=n, src=src, dst=dst, idx=idx, bound=n))
+        self.stream = torch.cuda.Stream(dev)
+        self.batch = None
+        self.per_call_ms = None
+        self.tuned = False
+
+    def tune(self):
+        self.tg.autotune_batch(self.tasks)
+        self.tuned = True
+
+    def build(self):
+        self.batch = self.tg.Batch(self.tasks)
+        with self.torch.cuda.stream(self.stream):
+            self.batch.capture(self.stream)
+
+    def verify(self):
+        torch = self.torch
+        if self.batch is None:
+            self.build()
+        for t in self.tasks:
+            t["dst"].fill_(SENTINEL)
+        self.batch.launch(self.stream)
+        self.stream.synchronize()
+        for k, t in enumerate(self.tasks):
+            n, w = t["n"], t["width"]
+            s, d = t["src"].view(n, w), t["dst"].view(n, w)
+            if t["op"] == 0:
+                ok = torch.equal(d, s)
+            elif t["op"] == 1:
+                ok = torch.equal(d, s[t["idx"].long()])
+            else:
+                ok = torch.equal(d[t["idx"].long()], s)
             if not ok:
-                raise SystemExit(f"bench verification failed: width {w} B, path {path}")
-    return written
+                raise SystemExit(f"bench verification failed: batch task {k}")
+
+    def bytes_per_step(self):
+        return self.batch.info()[1]
+
+    def launches_per_step(self):
+        return 1
+
+    def step(self, stream, events):
+        launch_with_events(self.torch, self.stream, events, "batch_kernel", lambda: self.batch.launch(self.stream))
+
+    def kernel_bytes(self, key):
+        return self.bytes_per_step()
+
+    def time_per_call(self, steps):
+        torch = self.torch
+        for _ in range(2):
+            self.tg.run_per_call(self.tasks, stream=self.stream)
+        self.stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(self.stream)
+        for _ in range(steps):
+            self.tg.run_per_call(self.tasks, stream=self.stream)
+        b.record(self.stream)
+        self.stream.synchronize()
+        self.per_call_ms = a.elapsed_time(b) / steps
+
+    def e2e(self, world, steps):
+        """Per step: pinned H2D of every source and index array, the batch,
+        pinned D2H of every destination.  Host memory bounds the sample: every
+        k-th array (k chosen so the pinned copies fit in a quarter of the
+        available host memory, at most 24 GB) forms its own batch."""
+        torch, tg = self.torch, self.tg
+        avail = host_mem_available()
+        budget = min(24 << 30, avail // 4) if avail else (8 << 30)
+        total = sum(2 * t["n"] * t["width"] + (4 * t["n"] if t["idx"] is not None else 0) for t in self.tasks)
+        stride = max(1, math.ceil(total / budget))
+        sub = self.tasks[::stride]
+        hs = [(t["src"].cpu().pin_memory(), t["idx"].cpu().pin_memory() if t["idx"] is not None else None,
+               torch.empty(t["dst"].numel(), dtype=torch.uint8).pin_memory()) for t in sub]
+        b = tg.Batch(sub)
+        sub_bytes = b.info()[1]
+        barrier(world)
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        with torch.cuda.stream(self.stream):
+            for _ in range(steps):
+                for t, (hsrc, hidx, hdst) in zip(sub, hs):
+                    t["src"].copy_(hsrc, non_blocking=True)
+                    h2d += hsrc.numel()
+                    if hidx is not None:
+                        t["idx"].copy_(hidx, non_blocking=True)
+                        h2d += hidx.numel() * 4
+                b.launch(self.stream)
+                for t, (_, _, hdst) in zip(sub, hs):
+                    hdst.copy_(t["dst"], non_blocking=True)
+                    d2h += hdst.numel()
+        self.stream.synchronize()
+        el = reduce_max(time.perf_counter() - t0, world, self.dev)
+        b.close()
+        return {"value": round(steps * sub_bytes * world / el / 1e9, 2), "unit": UNIT,
+                "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps, "steps": steps,
+                "sample": f"every {stride}th array ({len(sub)} arrays) as its own batch",
+                "path": "pinned H2D of all inputs, trv_batch_launch, pinned D2H of all outputs"}
+
+    def extra(self):
+        bps = self.bytes_per_step()
+        return {"tiles": self.batch.info()[0], "autotuned": self.tuned,
+                "per_call": {"ms_per_step": round(self.per_call_ms, 3),
+                             "value": round(bps / self.per_call_ms / 1e6, 2), "unit": UNIT,
+                             "launches_per_step": BATCH_COUNT},
+                "batched_vs_per_call": round(self.per_call_ms / self._batch_ms, 3)}
 
 
-def run_cpu_baseline(args, threads: int):
-    """The oracle's multithreaded port on a bounded sample of the sweep."""
+WORKLOADS = {"sweep": Sweep, "gather": Gather, "batch": Batch}
+
+
+# ---- CPU baseline (the oracle's multithreaded port) ----------------------------
+
+def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = None):
+    """(bytes moved, elapsed s, description) of the CPU form of the workload on
+    a bounded sample; runs `steps` passes if given, else passes until
+    `seconds` of work."""
     import numpy as np
 
     import oracle
-    sample_bytes = 128 << 20
-    src = oracle.random_words(sample_bytes // 4, 0, threads=threads).view(np.uint8)
-    dst = np.zeros_like(src)
-    plan = [(s, 4 * s, sample_bytes // (4 * s)) for s in WORDS]
-    total_bytes, elapsed, passes = 0, 0.0, 0
-    while elapsed < args.cpu_seconds or passes == 0:
-        for s, w, n in plan:
-            for _api in range(2):
-                t0 = time.perf_counter()
-                oracle.run_mt(oracle.OP_COPY_EXIT, dst, src, None, n, w, threads, modulus=MODULUS)
-                elapsed += time.perf_counter() - t0
-                total_bytes += 2 * n * w
+    if workload == "sweep":
+        sample = 128 << 20
+        src = oracle.random_words(sample // 4, 0, threads=threads).view(np.uint8)
+        dst = np.zeros_like(src)
+
+        def one():
+            done = 0
+            for s in WORDS:
+                w, n = 4 * s, sample // (4 * s)
+                for _api in range(2):
+                    oracle.run_mt(oracle.OP_COPY_EXIT, dst, src, None, n, w, threads, modulus=MODULUS)
+                    done += 2 * n * w
+            return done
+        desc = "the sweep on a 128 MiB array per width (both APIs), early-exit copy"
+    elif workload == "gather":
+        n = 1 << 21
+        src = oracle.random_words(n * 16, 0, threads=threads).view(np.uint8)
+        dst = np.zeros_like(src)
+        idxs = {"perm": oracle.permutation(n, 1), "runs": oracle.run_indices(n, 2),
+                "identity": np.arange(n, dtype=np.int32)}
+
+        def one():
+            done = 0
+            for w in GATHER_WIDTHS:
+                for p in GATHER_PATTERNS:
+                    oracle.run_mt(oracle.OP_GATHER, dst, src, idxs[p], n, w, threads)
+                    done += (2 * w + 4) * n
+            return done
+        desc = "the 21 gathers on 2^21 structs (1/8 of the workload's length)"
+    else:
+        rng = np.random.default_rng(4)
+        ops = rng.choice([0, 1, 2], size=BATCH_COUNT, p=[0.5, 0.4, 0.1])
+        widths = rng.choice(BATCH_WIDTHS, size=BATCH_COUNT)
+        lens = np.exp(rng.uniform(math.log(1 << 10), math.log(1 << 22), size=BATCH_COUNT)).astype(np.int64)
+        pick = list(range(0, BATCH_COUNT, 32))  # every 32nd array
+        arrays = []
+        for k in pick:
+            n, w = int(lens[k]), int(widths[k])
+            src = oracle.random_words(n * w // 4, 100 + k, threads=threads).view(np.uint8)
+            idx = oracle.uniform_indices(n, n, 200 + k) if ops[k] == 1 else (
+                oracle.permutation(n, 300 + k) if ops[k] == 2 else None)
+            arrays.append((int(ops[k]), n, w, src, np.zeros_like(src), idx))
+
+        def one():
+            done = 0
+            for op, n, w, src, dst, idx in arrays:
+                oracle.run_mt(op, dst, src, idx, n, w, threads)
+                done += 2 * n * w + (4 * n if op else 0)
+            return done
+        desc = "every 32nd array of the batch (128 arrays), same ops, widths and lengths"
+    one()  # warm caches and page in
+    total, el, passes = 0, 0.0, 0
+    while (steps is not None and passes < steps) or (steps is None and (el < seconds or passes == 0)):
+        t0 = time.perf_counter()
+        total += one()
+        el += time.perf_counter() - t0
         passes += 1
-    return {"value": total_bytes / elapsed / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{passes} passes of the sweep on a 128 MiB array per width (both APIs), "
-                      f"early-exit copy with the same predicate, {threads} threads"}
+    return total, el, f"{passes} passes of {desc}, {threads} threads (oracle port)"
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(args.workload, threads, 0, steps=1)
+    total, el, desc = cpu_sample(args.workload, threads, 0, steps=args.steps)
+    value = total / el / 1e9
+    cfg = WORKLOADS[args.workload].config
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded splitmix64 words)", "config": cfg,
+        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": desc + "; the reference has no CPU implementation of the path"},
+        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
 
 
 def run_trove(args, world, rank, local):
@@ -197,149 +637,55 @@ def run_trove(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     tg.load(build_if_missing=True)
-    plan = sweep_plan()
-    src = torch.empty(ARRAY_BYTES + 256, dtype=torch.uint8, device=dev)
-    dst = torch.empty_like(src)
-    tg.fill_random_u32(src, (ARRAY_BYTES + 256) // 4, seed=0)
-    written = {s: n for s, _, n in plan}
+    load_tune_cache(tg, args.tune_cache)
+    wl = WORKLOADS[args.workload](torch, tg, dev, args)
+    if not args.no_tune:
+        wl.tune()
+        save_tune_cache(tg, args.tune_cache)
+    if hasattr(wl, "build"):
+        wl.build()
     if not args.no_check:
-        written = verify_sweep(torch, tg, src, dst, plan)
-    bytes_per_step = sum(n * w + written[s] * w for s, w, n in plan) * 2
-    stream = torch.cuda.current_stream(dev)
-
-    def step(events=None):
-        for s, w, n in plan:
-            for path in (tg.PATH_WARP, tg.PATH_BLOCK):
-                if events is not None:
-                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    a.record(stream)
-                    tg.copy_exit(dst, src, n, w, MODULUS, path=path, stream=stream)
-                    b.record(stream)
-                    events.append(((s, path), a, b))
-                else:
-                    tg.copy_exit(dst, src, n, w, MODULUS, path=path, stream=stream)
-
+        wl.verify()
+    stream = wl.stream if hasattr(wl, "stream") else torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize(dev)
-    barrier(world)
-    torch.cuda.synchronize(dev)
-    clocks = Clocks(local)
-    events = []
-    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    for _ in range(args.steps):
-        step(events)
-    t_end.record(stream)
-    torch.cuda.synchronize(dev)
-    clock_info = clocks.stop()
-    barrier(world)
-    local_ms = t_start.elapsed_time(t_end)
-    ms = reduce_max(local_ms, world, dev)
-
-    # per-kernel launch durations (CUDA events on the launching stream)
-    per = {}
-    for key, a, b in events:
-        per.setdefault(key, []).append(a.elapsed_time(b))
+        wl.step(stream, None)
+    ms, events, clock_info = timed(torch, dev, stream, world, args.steps, lambda ev: wl.step(stream, ev))
     peak, peak_kind = hbm_peak()
-    kernels = []
-    for (s, path), times in per.items():
-        w, n = 4 * s, ARRAY_BYTES // (4 * s)
-        alg = n * w + written[s] * w
-        avg = sum(times) / len(times)
-        kernels.append({"kernel": f"copy_exit_{'warp' if path == tg.PATH_WARP else 'block'}_{w}B",
-                        "launches": len(times), "total_ms": round(sum(times), 3), "avg_ms": round(avg, 4),
-                        "bytes_per_launch": alg, "gbs": round(alg / avg / 1e6, 1),
-                        "frac": round(alg / avg / 1e6 / peak, 4)})
-    kernels.sort(key=lambda k: -k["total_ms"])
+    bps = wl.bytes_per_step()
+    value = bps * args.steps * world / (ms / 1e3) / 1e9
+    kernels = kernel_table(events, wl.kernel_bytes, peak)
     top = kernels[0]
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(top["kernel"])
-
-    # end to end through the host-buffer entry point (pinned in/out)
-    e2e = None
-    if args.e2e_steps > 0:
-        h_src = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
-        h_dst = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
-        h_src.copy_(src[:ARRAY_BYTES].cpu())
-        tg.copy_host(h_dst, h_src, ARRAY_BYTES // 64, 64)  # warm the staging buffers
-        barrier(world)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            for s, w, n in plan:
-                tg.copy_host(h_dst, h_src, n, w)
-        e2e_s = reduce_max(time.perf_counter() - t0, world, dev)
-        e2e_bytes = args.e2e_steps * sum(2 * n * w for s, w, n in plan) * world
-        if not torch.equal(h_dst[: plan[-1][2] * 64], h_src[: plan[-1][2] * 64]):
-            raise SystemExit("e2e verification failed")
-        per_step_io = sum(n * w for s, w, n in plan)
-        e2e = {"value": round(e2e_bytes / e2e_s / 1e9, 2), "unit": UNIT, "h2d_bytes_per_step": per_step_io,
-               "d2h_bytes_per_step": per_step_io, "steps": args.e2e_steps,
-               "path": "trv_copy_host per width (pinned host buffers, chunked H2D/kernel/D2H overlap)"}
-        del h_src, h_dst
-
-    cpu = run_cpu_baseline(args, os.cpu_count() or 1) if rank == 0 and world == 1 else None
-    value = bytes_per_step * args.steps * world / (ms / 1e3) / 1e9
+    if isinstance(wl, Batch):
+        wl._batch_ms = ms / args.steps
+        wl.time_per_call(max(3, args.steps // 3))
+    e2e = wl.e2e(world, args.e2e_steps) if args.e2e_steps > 0 else None
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:
+        total, el, desc = cpu_sample(args.workload, os.cpu_count() or 1, args.cpu_seconds)
+        cpu = {"value": round(total / el / 1e9, 2), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": desc}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64 words)",
-        "config": CONFIG,
+        "config": wl.config,
         "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak, "peak_kind": peak_kind,
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["gbs"], "peak": peak,
                      "unit": "GB/s", "frac": top["frac"], "traffic": traffic,
                      "bytes_per_launch": top["bytes_per_launch"], "peak_kind": f"of {peak_kind}"},
         "kernels": kernels,
         "e2e": e2e,
-        "gpu_launches": args.steps * len(plan) * 2,
+        "gpu_launches": args.steps * wl.launches_per_step(),
         "clocks": clock_info,
         "cpu_baseline": cpu,
+        "details": wl.extra(),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-
-
-# ---- the reference arm: the CPU form of the path ------------------------------
-
-def run_reference(args, world, rank):
-    if rank != 0:
-        return
-    import numpy as np
-
-    import oracle
-    threads = os.cpu_count() or 1
-    sample_bytes = 64 << 20
-    src = oracle.random_words(sample_bytes // 4, 0, threads=threads).view(np.uint8)
-    dst = np.zeros_like(src)
-    plan = [(s, 4 * s, sample_bytes // (4 * s)) for s in WORDS]
-
-    def step():
-        done = 0
-        for s, w, n in plan:
-            for _api in range(2):
-                oracle.run_mt(oracle.OP_COPY_EXIT, dst, src, None, n, w, threads, modulus=MODULUS)
-                done += 2 * n * w
-        return done
-
-    for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
-    total = sum(step() for _ in range(args.steps))
-    el = time.perf_counter() - t0
-    value = total / el / 1e9
-    sample = (f"each step: the sweep on a 64 MiB array per width (both APIs), early-exit copy, "
-              f"{threads} threads (oracle port: the reference has no CPU implementation)")
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el * 1e3 / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic (seeded splitmix64 words)", "config": CONFIG,
-        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }), flush=True)
 
 
 def main():

@@ -70,6 +70,9 @@ typedef struct trv_launch {
     int32_t grid_blocks;   /* 0: one pass per warp (full grid); -1: persistent grid of
                               resident blocks; > 0: that many blocks, grid-stride */
     int32_t chunk_bytes;   /* TRV_PATH_BULK: bytes per shared-memory stage, multiple of 16 */
+    int32_t cache_policy;  /* gather / scatter, TRV_PATH_WARP: 0 default; 1 streaming index and
+                              contiguous side (evict-first); 2 as 1, random side L2-only;
+                              3 as 1, random side kept in L2 (evict-last) */
 } trv_launch;
 
 const char* trv_status_string(int32_t status);
@@ -123,11 +126,90 @@ int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t
  * stream the CPU oracle generates).  No reference counterpart. */
 int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void* stream);
 
+/* Synthetic indices: idx[i] = uniform in [0, bound) from the seeded stream
+ * (the oracle's orc_uniform_indices gives the same values).  bound < 2^31. */
+int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint64_t seed, void* stream);
+
 /* Host-buffer copy: src_host -> device staging -> copy kernel -> dst_host,
  * chunked and overlapped on internal streams; returns when dst_host holds
  * the result.  Buffers should be pinned for full speed.  No reference
  * counterpart (the reference has no host API). */
 int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t n, uint32_t width);
+
+/* ---- batched execution ---------------------------------------------------
+ * Thousands of independent AoS arrays in one persistent launch driven by a
+ * device work queue.  No reference counterpart: the reference moves one array
+ * per user kernel. */
+
+typedef enum trv_op {
+    TRV_OP_COPY = 0,
+    TRV_OP_GATHER = 1,
+    TRV_OP_SCATTER = 2,
+    /* autotuner keys only: the early-exit copy through each device-API path */
+    TRV_OP_COPY_EXIT_WARP = 3,
+    TRV_OP_COPY_EXIT_BLOCK = 4
+} trv_op;
+
+typedef struct trv_task {
+    int32_t op;          /* trv_op */
+    uint32_t width;      /* bytes per struct: a multiple of 4, at most 64 */
+    uint64_t n;          /* structs copied, or number of indices */
+    const void* src;     /* device */
+    void* dst;           /* device */
+    const int32_t* idx;  /* device, n entries (gather / scatter only) */
+    uint64_t bound;      /* gather: source length; scatter: destination length */
+} trv_task;
+
+typedef struct trv_batch_options {
+    int32_t tile_bytes;  /* payload bytes per tile; 0: autotuner cache, else the size rule */
+    int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO, TRV_PATH_VECTOR or TRV_PATH_WARP */
+    int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
+} trv_batch_options;
+
+typedef struct trv_batch trv_batch;
+
+/* Validates the tasks, splits them into tiles and uploads the plan (device
+ * memory owned by the batch).  Pointers are captured, not the data: the batch
+ * may be launched any number of times while the arrays stay allocated. */
+int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
+                         trv_batch** out);
+/* Enqueues one run of the whole batch: counter reset + one persistent kernel,
+ * or a replay of the captured graph. */
+int32_t trv_batch_launch(trv_batch* batch, void* stream);
+/* Records counter reset + kernel into a CUDA graph (on `stream`, which must
+ * not be the legacy default stream); later trv_batch_launch calls replay it. */
+int32_t trv_batch_capture(trv_batch* batch, void* stream);
+/* Tiles and algorithmic bytes (read + written + index bytes) of one run. */
+int32_t trv_batch_info(const trv_batch* batch, uint64_t* tiles, uint64_t* bytes);
+int32_t trv_batch_destroy(trv_batch* batch);
+
+/* Baseline for the batch: one plain launch per task (trv_copy / trv_gather /
+ * trv_scatter, AUTO path), in order, on `stream`. */
+int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream);
+
+/* ---- autotuner -------------------------------------------------------------
+ * Launch choices cached per (scope, op, width, length bucket of a factor 4).
+ * Scope 0 (per call) steers the AUTO path of trv_copy / trv_gather /
+ * trv_scatter; scope 1 (batch) gives the batched kernel its tile size and copy
+ * variant.  No reference counterpart. */
+
+/* Times every candidate launch shape for (op, width, n) on scratch arrays of
+ * n structs (uniform random indices for gather / scatter; op may also be
+ * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625) and caches
+ * the fastest in scope 0. */
+int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream);
+/* Times tile sizes (and copy variants) for each (op, width, bucket) group of
+ * the given tasks, running each group alone as a batch, and caches the
+ * fastest in scope 1.  The tasks' arrays are read and written. */
+int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream);
+/* Cached choice for (scope, op, width, n); TRV_ERR_NOT_FOUND if none. */
+int32_t trv_autotune_lookup(int32_t scope, int32_t op, uint32_t width, uint64_t n, trv_launch* out,
+                            int32_t* tile_bytes);
+int32_t trv_autotune_clear(void);
+/* JSON file: an array of {scope, op, width, bucket, path, unroll, grid, chunk,
+ * tile_bytes, gbs} objects. */
+int32_t trv_autotune_save(const char* path);
+int32_t trv_autotune_load(const char* path);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,197 @@
+"""Batched execution (one persistent launch for many arrays) and the
+autotuner cache.  The cache tests run on CPU; batch tests need a GPU and check
+every task bit-exact against the oracle, launched plainly, as a CUDA graph
+replay, and against one launch per task."""
+import json
+
+import numpy as np
+import pytest
+
+import oracle
+import trove_gb300 as tg
+
+SENTINEL = 0xA5
+
+
+def test_autotune_cache_roundtrip(trove_lib, tmp_path):
+    tg.autotune_clear()
+    assert tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_COPY, 12, 1 << 20) is None
+    entries = [
+        {"scope": 0, "op": 0, "width": 12, "bucket": 10, "path": 3, "unroll": 4, "grid": 0, "chunk": 0,
+         "tile_bytes": 0, "cache_policy": 0, "gbs": 7100.0},
+        {"scope": 1, "op": 1, "width": 36, "bucket": 8, "path": 0, "unroll": 0, "grid": 0, "chunk": 0,
+         "tile_bytes": 131072, "cache_policy": 1, "gbs": 3000.5},
+        {"scope": 0, "op": 3, "width": 20, "bucket": 13, "path": 1, "unroll": 8, "grid": 0, "chunk": 0,
+         "tile_bytes": 0, "gbs": 6800.0},
+    ]
+    src = tmp_path / "in.json"
+    src.write_text(json.dumps(entries))
+    tg.autotune_load(src)
+    got, tile = tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_COPY, 12, 1 << 20)  # bucket(2^20) == 10
+    assert (got.path, got.unroll) == (3, 4) and tile == 0
+    got, tile = tg.autotune_lookup(tg.SCOPE_BATCH, tg.OP_GATHER, 36, 1 << 16)
+    assert tile == 131072 and got.cache_policy == 1
+    assert tg.autotune_lookup(tg.SCOPE_CALL, 3, 20, 1 << 26)[0].unroll == 8
+    assert tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_COPY, 12, 1 << 12) is None  # other bucket
+    out = tmp_path / "out.json"
+    tg.autotune_save(out)
+    back = {(e["scope"], e["op"], e["width"], e["bucket"]): e for e in json.loads(out.read_text())}
+    assert len(back) == 3
+    assert back[(1, 1, 36, 8)]["tile_bytes"] == 131072
+    assert back[(0, 3, 20, 13)]["unroll"] == 8
+    tg.autotune_clear()
+    assert tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_COPY, 12, 1 << 20) is None
+    with pytest.raises(tg.TroveError):
+        tg.autotune_load(tmp_path / "missing.json")
+
+
+def test_batch_argument_errors(trove_lib):
+    ok = 0x100000
+    bad_tasks = [
+        [dict(op=7, width=12, n=5, src=ok, dst=ok)],
+        [dict(op=0, width=13, n=5, src=ok, dst=ok)],
+        [dict(op=0, width=68, n=5, src=ok, dst=ok)],
+        [dict(op=0, width=12, n=5, src=0, dst=ok)],
+        [dict(op=1, width=12, n=5, src=ok, dst=ok, idx=None, bound=5)],
+        [dict(op=1, width=12, n=5, src=ok + 2, dst=ok, idx=ok, bound=5)],
+    ]
+    for tasks, status in zip(bad_tasks, [1, 2, 2, 1, 1, 3]):
+        with pytest.raises(tg.TroveError) as e:
+            tg.Batch(tasks)
+        assert e.value.status == status
+    with pytest.raises(tg.TroveError):
+        tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path="bulk")
+
+
+def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000):
+    """Mixed tasks with their expected outputs (oracle)."""
+    rng = np.random.default_rng(seed)
+    tasks, expect, outs = [], [], []
+    for k in range(count):
+        op = int(rng.choice([0, 0, 0, 0, 0, 1, 1, 1, 1, 2]))
+        w = int(rng.choice(widths))
+        n = int(np.exp(rng.uniform(np.log(1), np.log(max_len))))
+        if k % 17 == 0:
+            n = 0
+        src_h = oracle.random_structs(max(n, 1), w, seed=seed * 1000 + k)[:n]
+        init = np.full(max(n, 1) * w, SENTINEL, np.uint8)
+        src = torch.from_numpy(src_h.reshape(-1).copy()).cuda() if n else torch.zeros(w, dtype=torch.uint8,
+                                                                                        device="cuda")
+        dst = torch.from_numpy(init.copy()).cuda()
+        idx_t, bound = None, 0
+        if op == 0:
+            e = init.copy()
+            e[: n * w] = src_h.reshape(-1)
+        elif op == 1:
+            idx_h = oracle.uniform_indices(n, max(n, 1), seed + k) if n else np.zeros(1, np.int32)
+            if n > 10:
+                idx_h[3] = -1  # skipped
+                idx_h[7] = n + 5  # skipped
+            idx_t = torch.from_numpy(idx_h.copy()).cuda()
+            bound = n
+            e = init.copy().reshape(-1, w)
+            ok = (idx_h[:n] >= 0) & (idx_h[:n] < n)
+            e[:n][ok] = src_h[idx_h[:n][ok]]
+            e = e.reshape(-1)
+        else:
+            idx_h = oracle.permutation(n, seed + k) if n else np.zeros(1, np.int32)
+            idx_t = torch.from_numpy(idx_h.copy()).cuda()
+            bound = n
+            e = oracle.scatter(init, src_h, idx_h, n, w) if n else init.copy()
+        tasks.append(dict(op=op, width=w, n=n, src=src, dst=dst, idx=idx_t, bound=bound))
+        expect.append(e)
+        outs.append(dst)
+    return tasks, expect
+
+
+def reset(tasks):
+    for t in tasks:
+        t["dst"].fill_(SENTINEL)
+
+
+def check(tasks, expect):
+    for k, (t, e) in enumerate(zip(tasks, expect)):
+        got = t["dst"].cpu().numpy()
+        assert np.array_equal(got, e), (k, t["op"], t["width"], t["n"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("copy_path", ["vector", "warp", "auto"])
+@pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
+def test_batch_matches_oracle(cuda, copy_path, tile_bytes):
+    torch = cuda
+    tasks, expect = make_workload(torch, 120, seed=3)
+    b = tg.Batch(tasks, tile_bytes=tile_bytes, copy_path=copy_path)
+    tiles, nbytes = b.info()
+    assert tiles > 0 and nbytes > 0
+    b.launch()
+    torch.cuda.synchronize()
+    check(tasks, expect)
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_and_per_call(cuda):
+    torch = cuda
+    tasks, expect = make_workload(torch, 200, seed=9, widths=tuple(range(4, 65, 4)))
+    stream = torch.cuda.Stream()
+    b = tg.Batch(tasks, tile_bytes=8192)
+    with torch.cuda.stream(stream):
+        b.capture(stream)
+        for _ in range(3):
+            reset(tasks)
+            b.launch(stream)
+            stream.synchronize()
+            check(tasks, expect)
+    reset(tasks)
+    tg.run_per_call(tasks)
+    torch.cuda.synchronize()
+    check(tasks, expect)
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batch_grid_override_and_empty(cuda):
+    torch = cuda
+    tasks, expect = make_workload(torch, 40, seed=5)
+    for grid in [1, 3, 1000]:
+        reset(tasks)
+        tg.Batch(tasks, grid=grid, tile_bytes=2048).launch()
+        torch.cuda.synchronize()
+        check(tasks, expect)
+    empty = tg.Batch([])
+    assert empty.info() == (0, 0)
+    empty.launch()
+
+
+@pytest.mark.gpu
+def test_autotune_on_gpu(cuda, tmp_path):
+    torch = cuda
+    tg.autotune_clear()
+    n, w = 1 << 18, 12
+    for op in (tg.OP_COPY, tg.OP_GATHER, 3, 4):
+        tg.autotune_call(op, w, n)
+        assert tg.autotune_lookup(tg.SCOPE_CALL, op, w, n) is not None, op
+    src_h = oracle.random_structs(n, w, seed=1)
+    src = torch.from_numpy(src_h.reshape(-1).copy()).cuda()
+    dst = torch.zeros_like(src)
+    tg.copy(dst, src, n, w)  # AUTO consults the cache
+    idx_h = oracle.permutation(n, 2)
+    gd = torch.zeros_like(src)
+    tg.gather(gd, src, n, torch.from_numpy(idx_h).cuda(), n, w)
+    init = np.full(n * w, SENTINEL, np.uint8)
+    ed = torch.from_numpy(init).cuda()
+    tg.copy_exit(ed, src, n, w, 625, path="warp")
+    torch.cuda.synchronize()
+    assert np.array_equal(dst.cpu().numpy(), src_h.reshape(-1))
+    assert np.array_equal(gd.cpu().numpy(), oracle.gather(np.zeros(n * w, np.uint8), src_h, idx_h, n, w))
+    assert np.array_equal(ed.cpu().numpy(), oracle.copy_exit(init, src_h, n, w, 625)[0])
+    tasks, expect = make_workload(torch, 60, seed=11)
+    tg.autotune_batch(tasks)
+    reset(tasks)
+    tg.Batch(tasks).launch()
+    torch.cuda.synchronize()
+    check(tasks, expect)
+    tg.autotune_save(tmp_path / "cache.json")
+    assert json.loads((tmp_path / "cache.json").read_text())
+    tg.autotune_clear()

@@ -215,6 +215,14 @@ def test_fill_matches_oracle_stream(cuda):
         assert np.array_equal(to_host(t).view(np.uint32), oracle.random_words(nwords, seed))
 
 
+def test_uniform_indices_match_oracle(cuda):
+    torch = cuda
+    for n, bound, seed in [(1, 1, 0), (5000, 77, 3), (1 << 20, 1 << 20, 9)]:
+        t = torch.empty(n, dtype=torch.int32, device="cuda")
+        tg.fill_uniform_indices(t, n, bound, seed)
+        assert np.array_equal(to_host(t), oracle.uniform_indices(n, bound, seed))
+
+
 def test_copy_host(cuda):
     torch = cuda
     for n, width, pinned in [(1, 12, False), (100003, 12, True), ((96 << 20) // 28 + 5, 28, True)]:

@@ -50,7 +50,27 @@ class Launch(ctypes.Structure):
     """trv_launch: optional path / unroll / block / grid choice (0 = choose)."""
     _fields_ = [("path", ctypes.c_int32), ("unroll", ctypes.c_int32),
                 ("block_threads", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
-                ("chunk_bytes", ctypes.c_int32)]
+                ("chunk_bytes", ctypes.c_int32), ("cache_policy", ctypes.c_int32)]
+
+
+OP_COPY = 0
+OP_GATHER = 1
+OP_SCATTER = 2
+OP_COPY_EXIT_WARP = 3   # autotuner keys of the early-exit copy
+OP_COPY_EXIT_BLOCK = 4
+SCOPE_CALL = 0
+SCOPE_BATCH = 1
+
+
+class Task(ctypes.Structure):
+    """trv_task: one array of a batch."""
+    _fields_ = [("op", ctypes.c_int32), ("width", ctypes.c_uint32), ("n", ctypes.c_uint64),
+                ("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("idx", ctypes.c_void_p),
+                ("bound", ctypes.c_uint64)]
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("tile_bytes", ctypes.c_int32), ("copy_path", ctypes.c_int32), ("grid_blocks", ctypes.c_int32)]
 
 
 _lib = None
@@ -80,7 +100,24 @@ _SIGNATURES = {
                                         ctypes.c_void_p]),
     "trv_fill_random_u32": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                              ctypes.c_void_p]),
+    "trv_fill_uniform_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
+                                                  ctypes.c_void_p]),
     "trv_copy_host": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32]),
+    "trv_batch_create": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.POINTER(BatchOptions),
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "trv_batch_launch": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "trv_batch_capture": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "trv_batch_info": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                        ctypes.POINTER(ctypes.c_uint64)]),
+    "trv_batch_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
+    "trv_run_per_call": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_autotune_call": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_autotune_batch": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_autotune_lookup": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64,
+                                             ctypes.POINTER(Launch), ctypes.POINTER(ctypes.c_int32)]),
+    "trv_autotune_clear": (ctypes.c_int32, []),
+    "trv_autotune_save": (ctypes.c_int32, [ctypes.c_char_p]),
+    "trv_autotune_load": (ctypes.c_int32, [ctypes.c_char_p]),
 }
 
 
@@ -143,12 +180,12 @@ def _check(rc: int, where: str):
         raise TroveError(rc, where, detail)
 
 
-def _launch(path, unroll, block, grid, chunk=0):
+def _launch(path, unroll, block, grid, chunk=0, policy=0):
     if isinstance(path, str):
         path = PATHS[path]
-    if not (path or unroll or block or grid or chunk):
+    if not (path or unroll or block or grid or chunk or policy):
         return None
-    return ctypes.byref(Launch(int(path), int(unroll), int(block), int(grid), int(chunk)))
+    return ctypes.byref(Launch(int(path), int(unroll), int(block), int(grid), int(chunk), int(policy)))
 
 
 def copy(dst, src, n: int, width: int, *, path=PATH_AUTO, unroll: int = 0, block: int = 0, grid: int = 0,
@@ -169,23 +206,23 @@ def copy_exit(dst, src, n: int, width: int, modulus: int, *, path=PATH_WARP, unr
     """Copy skipping structs whose first word w has w % modulus == modulus - 1."""
     if isinstance(path, str):
         path = PATHS[path]
-    cfg = Launch(int(path), int(unroll), 0, int(grid), 0)
+    cfg = Launch(int(path), int(unroll), 0, int(grid), 0, 0)
     _check(load().trv_copy_exit_ex(_addr(dst), _addr(src), n, width, modulus, ctypes.byref(cfg), _stream(stream)),
            "trv_copy_exit")
 
 
 def gather(dst, src, src_n: int, idx, n: int, width: int, *, path=PATH_AUTO, unroll: int = 0, block: int = 0,
-           grid: int = 0, stream=None):
+           grid: int = 0, policy: int = 0, stream=None):
     """dst[i] = src[idx[i]] (trv_gather_ex); out-of-range indices are skipped."""
     _check(load().trv_gather_ex(_addr(dst), _addr(src), src_n, _addr(idx), n, width,
-                                _launch(path, unroll, block, grid), _stream(stream)), "trv_gather")
+                                _launch(path, unroll, block, grid, 0, policy), _stream(stream)), "trv_gather")
 
 
 def scatter(dst, dst_n: int, src, idx, n: int, width: int, *, path=PATH_AUTO, unroll: int = 0, block: int = 0,
-            grid: int = 0, stream=None):
+            grid: int = 0, policy: int = 0, stream=None):
     """dst[idx[i]] = src[i] (trv_scatter_ex); out-of-range indices are skipped."""
     _check(load().trv_scatter_ex(_addr(dst), dst_n, _addr(src), _addr(idx), n, width,
-                                 _launch(path, unroll, block, grid), _stream(stream)), "trv_scatter")
+                                 _launch(path, unroll, block, grid, 0, policy), _stream(stream)), "trv_scatter")
 
 
 def fill_random_u32(dst, nwords: int, seed: int, *, stream=None):
@@ -193,6 +230,102 @@ def fill_random_u32(dst, nwords: int, seed: int, *, stream=None):
     _check(load().trv_fill_random_u32(_addr(dst), nwords, seed, _stream(stream)), "trv_fill_random_u32")
 
 
+def fill_uniform_indices(idx, n: int, bound: int, seed: int, *, stream=None):
+    """idx[i] uniform in [0, bound) from the seeded stream (same as the oracle)."""
+    _check(load().trv_fill_uniform_indices(_addr(idx), n, bound, seed, _stream(stream)), "trv_fill_uniform_indices")
+
+
 def copy_host(dst_host, src_host, n: int, width: int):
     """Host-buffer copy through the device; returns when dst_host is written."""
     _check(load().trv_copy_host(_addr(dst_host), _addr(src_host), n, width), "trv_copy_host")
+
+
+# ---- batched execution -------------------------------------------------------
+
+def make_tasks(tasks) -> "ctypes.Array":
+    """Task array from Task objects or dicts with keys op, width, n, src, dst,
+    idx, bound (addresses may be tensors)."""
+    arr = (Task * len(tasks))()
+    for k, t in enumerate(tasks):
+        if isinstance(t, Task):
+            arr[k] = t
+            continue
+        arr[k] = Task(int(t["op"]), int(t["width"]), int(t["n"]), _addr(t["src"]), _addr(t["dst"]),
+                      _addr(t.get("idx")), int(t.get("bound", 0)))
+    return arr
+
+
+class Batch:
+    """A planned batch (trv_batch): launch() runs every task in one
+    persistent kernel; capture() records it as a CUDA graph first."""
+
+    def __init__(self, tasks, *, tile_bytes: int = 0, copy_path=PATH_AUTO, grid: int = 0):
+        if isinstance(copy_path, str):
+            copy_path = PATHS[copy_path]
+        self._tasks = make_tasks(tasks)
+        opt = BatchOptions(int(tile_bytes), int(copy_path), int(grid))
+        h = ctypes.c_void_p()
+        _check(load().trv_batch_create(self._tasks, len(self._tasks), ctypes.byref(opt), ctypes.byref(h)),
+               "trv_batch_create")
+        self._h = h
+
+    def launch(self, stream=None):
+        _check(load().trv_batch_launch(self._h, _stream(stream)), "trv_batch_launch")
+
+    def capture(self, stream):
+        _check(load().trv_batch_capture(self._h, _stream(stream)), "trv_batch_capture")
+
+    def info(self):
+        tiles, nbytes = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(load().trv_batch_info(self._h, ctypes.byref(tiles), ctypes.byref(nbytes)), "trv_batch_info")
+        return tiles.value, nbytes.value
+
+    def close(self):
+        if self._h:
+            _check(load().trv_batch_destroy(self._h), "trv_batch_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_per_call(tasks, stream=None):
+    """One plain launch per task (the batch's baseline)."""
+    arr = make_tasks(tasks)
+    _check(load().trv_run_per_call(arr, len(arr), _stream(stream)), "trv_run_per_call")
+
+
+# ---- autotuner ----------------------------------------------------------------
+
+def autotune_call(op: int, width: int, n: int, stream=None):
+    _check(load().trv_autotune_call(op, width, n, _stream(stream)), "trv_autotune_call")
+
+
+def autotune_batch(tasks, stream=None):
+    arr = make_tasks(tasks)
+    _check(load().trv_autotune_batch(arr, len(arr), _stream(stream)), "trv_autotune_batch")
+
+
+def autotune_lookup(scope: int, op: int, width: int, n: int):
+    """(Launch, tile_bytes) cached for the key, or None."""
+    out, tile = Launch(), ctypes.c_int32()
+    rc = load().trv_autotune_lookup(scope, op, width, n, ctypes.byref(out), ctypes.byref(tile))
+    if rc == 8:
+        return None
+    _check(rc, "trv_autotune_lookup")
+    return out, tile.value
+
+
+def autotune_clear():
+    _check(load().trv_autotune_clear(), "trv_autotune_clear")
+
+
+def autotune_save(path):
+    _check(load().trv_autotune_save(str(path).encode()), "trv_autotune_save")
+
+
+def autotune_load(path):
+    _check(load().trv_autotune_load(str(path).encode()), "trv_autotune_load")

@@ -1,0 +1,216 @@
+// Host side of batched execution: validation, the tile plan, the device task
+// table, graph capture, and the one-launch-per-task baseline.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+#include <new>
+#include <vector>
+
+#include "autotune.h"
+#include "batch.h"
+#include "runtime.h"
+#include "trove_gb300.h"
+
+struct trv_batch {
+    int device = 0;
+    int ntasks = 0;
+    trv::BatchTask* d_tasks = nullptr;
+    long long* d_prefix = nullptr;
+    unsigned long long* d_counter = nullptr;
+    long long total_tiles = 0;
+    uint64_t bytes = 0;
+    int grid = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+bool aligned4(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; }
+
+int validate(const trv_task& t) {
+    if (t.op < TRV_OP_COPY || t.op > TRV_OP_SCATTER) return TRV_ERR_INVALID_ARGUMENT;
+    if (t.width == 0 || t.n > (uint64_t(1) << 62) / t.width || t.bound > (uint64_t(1) << 62) / t.width)
+        return TRV_ERR_INVALID_ARGUMENT;
+    if (t.width % 4 != 0 || t.width > 64) return TRV_ERR_UNSUPPORTED;
+    if (t.n == 0) return TRV_OK;
+    if (!t.src || !t.dst) return TRV_ERR_INVALID_ARGUMENT;
+    if (!aligned4(t.src) || !aligned4(t.dst)) return TRV_ERR_MISALIGNED;
+    if (t.op != TRV_OP_COPY) {
+        if (!t.idx) return TRV_ERR_INVALID_ARGUMENT;
+        if (!aligned4(t.idx)) return TRV_ERR_MISALIGNED;
+    }
+    return TRV_OK;
+}
+
+// Size rule when no tuned tile exists: big enough to amortise the queue
+// step, small enough to balance the tail across 152 SMs.
+int default_tile_bytes(int op) { return op == TRV_OP_COPY ? (128 << 10) : (64 << 10); }
+
+void release(trv_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_tasks) cudaFree(b->d_tasks);
+    if (b->d_prefix) cudaFree(b->d_prefix);
+    if (b->d_counter) cudaFree(b->d_counter);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->d_tasks = nullptr;
+    b->d_prefix = nullptr;
+    b->d_counter = nullptr;
+}
+
+}  // namespace
+
+using namespace trv;
+
+extern "C" {
+
+int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_options* opt, trv_batch** out) {
+    if (!out) return TRV_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
+    if (count >= uint64_t(INT_MAX)) return TRV_ERR_INVALID_ARGUMENT;
+    if (opt && opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR &&
+        opt->copy_path != TRV_PATH_WARP)
+        return TRV_ERR_UNSUPPORTED;
+    if (opt && opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
+    std::vector<BatchTask> host(count);
+    std::vector<long long> prefix(count + 1, 0);
+    uint64_t bytes = 0;
+    for (uint64_t k = 0; k < count; ++k) {
+        const trv_task& t = tasks[k];
+        const int rc = validate(t);
+        if (rc != TRV_OK) return rc;
+        TuneChoice c;
+        const TuneKey key{SCOPE_BATCH, t.op, int(t.width), len_bucket(t.n)};
+        const bool tuned = tune_lookup(key, &c);
+        int tile_bytes = (opt && opt->tile_bytes > 0) ? opt->tile_bytes
+                         : (tuned && c.tile_bytes > 0) ? c.tile_bytes
+                                                       : default_tile_bytes(t.op);
+        long long tile = (long long)tile_bytes / t.width;
+        tile = tile < 32 ? 32 : (tile / 32) * 32;
+        if (tile > (1 << 30)) tile = 1 << 30;
+        int variant = (opt && opt->copy_path != TRV_PATH_AUTO) ? opt->copy_path
+                      : (tuned && c.path != 0)                  ? c.path
+                                                                : TRV_PATH_VECTOR;
+        BatchTask& d = host[k];
+        d.src = static_cast<const unsigned char*>(t.src);
+        d.dst = static_cast<unsigned char*>(t.dst);
+        d.idx = t.idx;
+        d.n = (long long)t.n;
+        d.bound = (long long)t.bound;
+        d.op = t.op;
+        d.words = int(t.width / 4);
+        d.tile_structs = int(tile);
+        d.variant = variant;
+        prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
+        bytes += 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
+    }
+    trv_batch* b = new (std::nothrow) trv_batch;
+    if (!b) return TRV_ERR_OUT_OF_MEMORY;
+    cudaGetDevice(&b->device);
+    b->ntasks = int(count);
+    b->total_tiles = prefix[count];
+    b->bytes = bytes;
+    cudaError_t e = cudaMalloc(&b->d_tasks, sizeof(BatchTask) * (count ? count : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(long long) * (count + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_counter, sizeof(unsigned long long));
+    if (e == cudaSuccess && count)
+        e = cudaMemcpy(b->d_tasks, host.data(), sizeof(BatchTask) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * (count + 1), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        release(b);
+        delete b;
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? TRV_ERR_OUT_OF_MEMORY : cuda_fail(e);
+    }
+    const int resident = resident_blocks(batch_kernel_func(), batch_block_threads());
+    b->grid = (opt && opt->grid_blocks > 0) ? opt->grid_blocks : resident;
+    if (b->total_tiles < b->grid) b->grid = b->total_tiles > 0 ? int(b->total_tiles) : 1;
+    *out = b;
+    return TRV_OK;
+}
+
+int32_t trv_batch_launch(trv_batch* b, void* stream) {
+    if (!b) return TRV_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (b->exec) {
+        const cudaError_t e = cudaGraphLaunch(b->exec, st);
+        return e == cudaSuccess ? TRV_OK : cuda_fail(e);
+    }
+    if (b->total_tiles == 0) return TRV_OK;
+    cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return cuda_fail(e);
+    e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, st);
+    return e == cudaSuccess ? TRV_OK : cuda_fail(e);
+}
+
+int32_t trv_batch_capture(trv_batch* b, void* stream) {
+    if (!b || !stream) return TRV_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+    }
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e);
+    int rc = TRV_OK;
+    if (b->total_tiles > 0) {
+        e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), st);
+        if (e == cudaSuccess) e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, st);
+        if (e != cudaSuccess) rc = cuda_fail(e);
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (rc != TRV_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e);
+    cudaGraphExec_t x = nullptr;
+    e = cudaGraphInstantiate(&x, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(e);
+    }
+    b->graph = g;
+    b->exec = x;
+    return TRV_OK;
+}
+
+int32_t trv_batch_info(const trv_batch* b, uint64_t* tiles, uint64_t* bytes) {
+    if (!b) return TRV_ERR_INVALID_ARGUMENT;
+    if (tiles) *tiles = uint64_t(b->total_tiles);
+    if (bytes) *bytes = b->bytes;
+    return TRV_OK;
+}
+
+int32_t trv_batch_destroy(trv_batch* b) {
+    if (!b) return TRV_ERR_INVALID_ARGUMENT;
+    release(b);
+    delete b;
+    return TRV_OK;
+}
+
+int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream) {
+    if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
+    for (uint64_t k = 0; k < count; ++k) {
+        const trv_task& t = tasks[k];
+        int rc;
+        switch (t.op) {
+            case TRV_OP_COPY: rc = trv_copy(t.dst, t.src, t.n, t.width, stream); break;
+            case TRV_OP_GATHER: rc = trv_gather(t.dst, t.src, t.bound, t.idx, t.n, t.width, stream); break;
+            case TRV_OP_SCATTER: rc = trv_scatter(t.dst, t.bound, t.src, t.idx, t.n, t.width, stream); break;
+            default: rc = TRV_ERR_INVALID_ARGUMENT;
+        }
+        if (rc != TRV_OK) return rc;
+    }
+    return TRV_OK;
+}
+
+}  // extern "C"

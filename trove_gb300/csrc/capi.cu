@@ -7,6 +7,7 @@
 #include <mutex>
 #include <unordered_map>
 
+#include "autotune.h"
 #include "bulk.h"
 #include "flat.h"
 #include "ops.h"
@@ -158,11 +159,14 @@ int copy_bulk(void* dst, const void* src, uint64_t nbytes, int chunk, int grid_r
     return e == cudaSuccess ? TRV_OK : cuda_fail(e);
 }
 
-// Measured on GB300: the TMA bulk engine moves long contiguous runs at the
-// copy roofline; it needs src == dst (mod 16), else the flat vector copy.
+// Without a tuned entry: the flat vector copy with one pass per warp, which
+// measured fastest on GB300 for every width (7.1 TB/s on 2 GiB arrays, above
+// the TMA bulk path's 6.8 TB/s and the device-API kernels' 6.3-7.2 TB/s).
 int pick_copy_path(const void* dst, const void* src, uint32_t width) {
+    (void)dst;
+    (void)src;
     (void)width;
-    return bulk_copy_supported(src, dst) ? TRV_PATH_BULK : TRV_PATH_VECTOR;
+    return TRV_PATH_VECTOR;
 }
 
 }  // namespace
@@ -212,13 +216,22 @@ int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, cons
     if (n == 0) return TRV_OK;
     if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int path = cfg ? cfg->path : TRV_PATH_AUTO;
-    const int unroll = cfg ? cfg->unroll : 0;
-    const int grid_req = cfg ? cfg->grid_blocks : 0;
-    if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
-    if (path == TRV_PATH_AUTO) path = pick_copy_path(dst, src, width);
+    trv_launch c = cfg ? *cfg : trv_launch{TRV_PATH_AUTO, 0, 0, 0, 0};
+    if (c.block_threads != 0 && c.block_threads != 256) return TRV_ERR_UNSUPPORTED;
+    if (c.path == TRV_PATH_AUTO) {
+        TuneChoice t;
+        if (tune_lookup(TuneKey{SCOPE_CALL, TRV_OP_COPY, int(width), len_bucket(n)}, &t) &&
+            (t.path != TRV_PATH_BULK || bulk_copy_supported(src, dst)) &&
+            (t.path != TRV_PATH_WARP || (struct_width(width) && aligned(dst, 4) && aligned(src, 4))))
+            c = trv_launch{t.path, t.unroll, 0, t.grid, t.chunk, 0};
+        else
+            c.path = pick_copy_path(dst, src, width);
+    }
+    int path = c.path;
+    const int unroll = c.unroll;
+    const int grid_req = c.grid_blocks;
     if (path == TRV_PATH_VECTOR) return copy_flat(dst, src, n * width, unroll, grid_req, st);
-    if (path == TRV_PATH_BULK) return copy_bulk(dst, src, n * width, cfg ? cfg->chunk_bytes : 0, grid_req, st);
+    if (path == TRV_PATH_BULK) return copy_bulk(dst, src, n * width, c.chunk_bytes, grid_req, st);
     if (path != TRV_PATH_WARP && path != TRV_PATH_BLOCK && path != TRV_PATH_DIRECT) return TRV_ERR_UNSUPPORTED;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
@@ -245,18 +258,28 @@ int32_t trv_copy_exit_ex(void* dst, const void* src, uint64_t n, uint32_t width,
     if (cfg->path != TRV_PATH_WARP && cfg->path != TRV_PATH_BLOCK) return TRV_ERR_UNSUPPORTED;
     if (cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
-    const int u = cfg->unroll > 0 ? cfg->unroll : default_unroll(width);
+    int u = cfg->unroll, grid_req = cfg->grid_blocks;
+    if (u == 0) {
+        TuneChoice t;
+        const int op = cfg->path == TRV_PATH_WARP ? TRV_OP_COPY_EXIT_WARP : TRV_OP_COPY_EXIT_BLOCK;
+        if (tune_lookup(TuneKey{SCOPE_CALL, op, int(width), len_bucket(n)}, &t)) {
+            u = t.unroll;
+            if (grid_req == 0) grid_req = t.grid;
+        } else {
+            u = default_unroll(width);
+        }
+    }
     const int slot = unroll_slot(u);
     if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
     const CopyKernel& k = ops_for_words(int(width / 4))->copy_exit[cfg->path == TRV_PATH_WARP ? 0 : 1][slot];
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, cfg->grid_blocks);
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
     k.launch(CopyArgs{src, dst, (long long)n, modulus}, grid, 256, static_cast<cudaStream_t>(stream));
     return check_launch();
 }
 
 int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, uint32_t modulus, int32_t path,
                       void* stream) {
-    trv_launch cfg = {path, 0, 0, 0, 0};
+    trv_launch cfg = {path, 0, 0, 0, 0, 0};
     return trv_copy_exit_ex(dst, src, n, width, modulus, &cfg, stream);
 }
 
@@ -266,12 +289,22 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
     if (n == 0) return TRV_OK;
     if (!dst || !src || !idx) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int path = cfg ? cfg->path : TRV_PATH_AUTO;
-    const int grid_req = cfg ? cfg->grid_blocks : 0;
-    if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
+    trv_launch c = cfg ? *cfg : trv_launch{TRV_PATH_AUTO, 0, 0, 0, 0};
+    if (c.block_threads != 0 && c.block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
     const bool structs = struct_width(width) && aligned(dst, 4) && aligned(src, 4);
-    if (path == TRV_PATH_AUTO) path = structs ? TRV_PATH_WARP : TRV_PATH_VECTOR;
+    if (c.path == TRV_PATH_AUTO) {
+        TuneChoice t;
+        if (structs && tune_lookup(TuneKey{SCOPE_CALL, gather ? TRV_OP_GATHER : TRV_OP_SCATTER, int(width),
+                                           len_bucket(n)},
+                                   &t))
+            c = trv_launch{t.path, t.unroll, 0, t.grid, 0, t.cache_policy};
+        else
+            c.path = structs ? TRV_PATH_WARP : TRV_PATH_VECTOR;
+    }
+    if (c.cache_policy < 0 || c.cache_policy > 3) return TRV_ERR_INVALID_ARGUMENT;
+    const int path = c.path;
+    const int grid_req = c.grid_blocks;
     if (path == TRV_PATH_VECTOR) {  // generic byte-wise form
         const long long blocks = (long long)((n + 255) / 256);
         const int cap = device_info().sm_count * 8;
@@ -285,7 +318,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
     if (path != TRV_PATH_COALESCED && path != TRV_PATH_DIRECT && path != TRV_PATH_WARP) return TRV_ERR_UNSUPPORTED;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
-    const int u = (cfg && cfg->unroll > 0) ? cfg->unroll : default_unroll(width);
+    const int u = c.unroll > 0 ? c.unroll : default_unroll(width);
     const int slot = unroll_slot(u);
     if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
     const WidthOps* ops = ops_for_words(int(width / 4));
@@ -300,7 +333,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
     }
     const IndexKernel& k = *kp;
     const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
-    k.launch(IndexArgs{src, dst, idx, (long long)n, (long long)bound}, grid, 256, st);
+    k.launch(IndexArgs{src, dst, idx, (long long)n, (long long)bound, c.cache_policy}, grid, 256, st);
     return check_launch();
 }
 
@@ -322,6 +355,15 @@ int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t
 int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n, uint32_t width,
                     void* stream) {
     return index_op(false, dst, src, dst_n, idx, n, width, nullptr, stream);
+}
+
+int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint64_t seed, void* stream) {
+    if (n == 0) return TRV_OK;
+    if (!idx || bound == 0 || bound > 0x7FFFFFFFu || n > (uint64_t(1) << 61)) return TRV_ERR_INVALID_ARGUMENT;
+    if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
+    launch_uniform_indices(idx, (long long)n, bound, seed, device_info().sm_count * 8,
+                           static_cast<cudaStream_t>(stream));
+    return check_launch();
 }
 
 int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void* stream) {

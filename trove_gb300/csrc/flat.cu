@@ -27,6 +27,22 @@ void launch_fill_u32(unsigned* dst, long long nwords, unsigned long long seed, i
     fill_u32_kernel<<<grid, 256, 0, st>>>(dst, nwords, seed);
 }
 
+// idx[i] = floor(word(seed, i) * bound / 2^32), the oracle's bounded draw.
+__global__ void uniform_indices_kernel(int* __restrict__ idx, long long n, unsigned bound, unsigned long long seed) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const unsigned w = (unsigned)(mix64((unsigned long long)k * 0x9E3779B97F4A7C15ull +
+                                            seed * 0xD1B54A32D192ED03ull + 1ull) >>
+                                      32);
+        idx[k] = (int)(((unsigned long long)w * bound) >> 32);
+    }
+}
+
+void launch_uniform_indices(int* idx, long long n, unsigned bound, unsigned long long seed, int grid,
+                            cudaStream_t st) {
+    uniform_indices_kernel<<<grid, 256, 0, st>>>(idx, n, bound, seed);
+}
+
 // ---- flat vector copy ----------------------------------------------------
 // Copies nbytes from s to d.  The first `head` bytes bring both pointers to
 // V alignment; the aligned middle moves as V vectors, U per thread per pass

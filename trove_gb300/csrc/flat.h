@@ -6,6 +6,8 @@
 namespace trv {
 
 void launch_fill_u32(unsigned* dst, long long nwords, unsigned long long seed, int grid, cudaStream_t st);
+void launch_uniform_indices(int* idx, long long n, unsigned bound, unsigned long long seed, int grid,
+                            cudaStream_t st);
 
 // Flat copy of nbytes: `head` leading bytes (< vec_bytes) bring both pointers
 // to vec_bytes alignment, the rest moves as vec_bytes vectors.

@@ -221,6 +221,78 @@ scatter_kernel(const aos<S>* __restrict__ src, const int* __restrict__ idx, aos<
     }
 }
 
+// ---- cache policies of the row-form kernels ----------------------------
+// 0: default (read-only path for loads, plain stores)
+// 1: the index stream and the contiguous side are streamed (evict-first), so
+//    L2 keeps the random side's sectors: structs narrower than a 32-byte
+//    sector share sectors, and a sector that stays in L2 is fetched once
+// 2: as 1, and the random side bypasses L1 (L2 only)
+// 3: as 1, and the random side is marked evict-last in L2
+__device__ __forceinline__ unsigned long long l2_evict_last_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ int ld_index(const int* p, int policy) { return policy ? __ldcs(p) : __ldg(p); }
+
+__device__ __forceinline__ uint4 ld_hint(const uint4* p, unsigned long long pol) {
+    uint4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ uint2 ld_hint(const uint2* p, unsigned long long pol) {
+    uint2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ unsigned ld_hint(const unsigned* p, unsigned long long pol) {
+    unsigned v;
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_hint(uint4* p, uint4 v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st_hint(uint2* p, uint2 v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.v2.u32 [%0], {%1, %2}, %3;" ::"l"(p), "r"(v.x), "r"(v.y), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st_hint(unsigned* p, unsigned v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
+template <typename V>
+__device__ __forceinline__ V ld_random(const V* p, int policy, unsigned long long pol) {
+    if (policy == 3) return ld_hint(p, pol);
+    if (policy == 2) return __ldcg(p);
+    return __ldg(p);
+}
+template <typename V>
+__device__ __forceinline__ V ld_contig(const V* p, int policy) {
+    return policy ? __ldcs(p) : __ldg(p);
+}
+template <typename V>
+__device__ __forceinline__ void st_random(V* p, V v, int policy, unsigned long long pol) {
+    if (policy == 3)
+        st_hint(p, v, pol);
+    else if (policy == 2)
+        __stcg(p, v);
+    else
+        *p = v;
+}
+template <typename V>
+__device__ __forceinline__ void st_contig(V* p, V v, int policy) {
+    if (policy)
+        __stcs(p, v);
+    else
+        *p = v;
+}
+
 // Row-form gather / scatter (TRV_PATH_WARP for index ops).  The C ABI knows
 // both sides of the operation, and one side is contiguous, so no struct ever
 // needs to sit in one lane: the warp moves 32 structs as m = 4S/sizeof(V)
@@ -233,16 +305,17 @@ scatter_kernel(const aos<S>* __restrict__ src, const int* __restrict__ idx, aos<
 template <int S, typename V, int U>
 __global__ void __launch_bounds__(256)
 gather_rows_kernel(const V* __restrict__ src, long long src_n, const int* __restrict__ idx, V* __restrict__ dst,
-                   long long n) {
+                   long long n, int policy) {
     constexpr int m = S * 4 / int(sizeof(V));
     const WarpGrid g;
     constexpr int CH = 32 * U;
+    const unsigned long long pol = policy == 3 ? l2_evict_last_policy() : 0ull;
     for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
         int id[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const long long i = base + u * 32 + g.lane;
-            const int v = i < n ? __ldg(idx + i) : -1;
+            const int v = i < n ? ld_index(idx + i, policy) : -1;
             id[u] = (v >= 0 && (long long)v < src_n) ? v : -1;
         }
         V val[U][m];
@@ -254,14 +327,14 @@ gather_rows_kernel(const V* __restrict__ src, long long src_n, const int* __rest
                 const int q = g.lane + 32 * k;
                 const int j = q / m;
                 from[u][k] = __shfl_sync(0xFFFFFFFFu, id[u], j);
-                if (from[u][k] >= 0) val[u][k] = __ldg(src + (long long)from[u][k] * m + (q - j * m));
+                if (from[u][k] >= 0) val[u][k] = ld_random(src + (long long)from[u][k] * m + (q - j * m), policy, pol);
             }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
 #pragma unroll
             for (int k = 0; k < m; ++k)
-                if (from[u][k] >= 0) dst[(base + u * 32) * m + g.lane + 32 * k] = val[u][k];
+                if (from[u][k] >= 0) st_contig(dst + (base + u * 32) * m + g.lane + 32 * k, val[u][k], policy);
         }
     }
 }
@@ -269,16 +342,17 @@ gather_rows_kernel(const V* __restrict__ src, long long src_n, const int* __rest
 template <int S, typename V, int U>
 __global__ void __launch_bounds__(256)
 scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* __restrict__ dst, long long dst_n,
-                    long long n) {
+                    long long n, int policy) {
     constexpr int m = S * 4 / int(sizeof(V));
     const WarpGrid g;
     constexpr int CH = 32 * U;
+    const unsigned long long pol = policy == 3 ? l2_evict_last_policy() : 0ull;
     for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
         int id[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const long long i = base + u * 32 + g.lane;
-            const int v = i < n ? __ldg(idx + i) : -1;
+            const int v = i < n ? ld_index(idx + i, policy) : -1;
             id[u] = (v >= 0 && (long long)v < dst_n) ? v : -1;
         }
         V val[U][m];
@@ -289,7 +363,7 @@ scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* _
             for (int k = 0; k < m; ++k) {
                 const int q = g.lane + 32 * k;
                 to[u][k] = __shfl_sync(0xFFFFFFFFu, id[u], q / m);
-                if (to[u][k] >= 0) val[u][k] = __ldg(src + (base + u * 32) * m + q);
+                if (to[u][k] >= 0) val[u][k] = ld_contig(src + (base + u * 32) * m + q, policy);
             }
         }
 #pragma unroll
@@ -297,7 +371,7 @@ scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* _
 #pragma unroll
             for (int k = 0; k < m; ++k) {
                 const int q = g.lane + 32 * k;
-                if (to[u][k] >= 0) dst[(long long)to[u][k] * m + (q - (q / m) * m)] = val[u][k];
+                if (to[u][k] >= 0) st_random(dst + (long long)to[u][k] * m + (q - (q / m) * m), val[u][k], policy, pol);
             }
         }
     }

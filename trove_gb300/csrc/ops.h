@@ -23,6 +23,7 @@ struct IndexArgs {
     const int* idx;
     long long n;
     long long bound;  // src_n for gather, dst_n for scatter
+    int policy;       // cache policy of the row-form kernels
 };
 
 template <typename Args>

@@ -65,13 +65,13 @@ struct word_of<4> {
 template <typename V, int U>
 void launch_gather_rows(const IndexArgs& a, int grid, int block, cudaStream_t st) {
     gather_rows_kernel<S, V, U><<<grid, block, 0, st>>>(static_cast<const V*>(a.src), a.bound, a.idx,
-                                                        static_cast<V*>(a.dst), a.n);
+                                                        static_cast<V*>(a.dst), a.n, a.policy);
 }
 
 template <typename V, int U>
 void launch_scatter_rows(const IndexArgs& a, int grid, int block, cudaStream_t st) {
     scatter_rows_kernel<S, V, U><<<grid, block, 0, st>>>(static_cast<const V*>(a.src), a.idx,
-                                                         static_cast<V*>(a.dst), a.bound, a.n);
+                                                         static_cast<V*>(a.dst), a.bound, a.n, a.policy);
 }
 
 template <typename V, int k>
