@@ -61,11 +61,13 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["trove", "reference"], default="trove")
-    p.add_argument("--workload", choices=["sweep", "gather", "batch"], default="sweep")
+    p.add_argument("--workload", choices=["sweep", "gather", "batch", "serve"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-check", action="store_true")
     p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--array-mib", type=int, default=ARRAY_BYTES >> 20,
+                   help="sweep: bytes per array in MiB (default 2048; smaller only for profiling)")
     p.add_argument("--tune-cache", default=os.environ.get(
         "TROVE_GB300_TUNE_CACHE", str(Path.home() / ".cache" / "trove_gb300" / "autotune.json")))
     return p.parse_args()
@@ -239,10 +241,14 @@ class Sweep:
 
     def __init__(self, torch, tg, dev, args):
         self.torch, self.tg, self.dev = torch, tg, dev
-        self.plan = [(s, 4 * s, ARRAY_BYTES // (4 * s)) for s in WORDS]
-        self.src = torch.empty(ARRAY_BYTES + 256, dtype=torch.uint8, device=dev)
+        self.array_bytes = args.array_mib << 20
+        self.plan = [(s, 4 * s, self.array_bytes // (4 * s)) for s in WORDS]
+        self.src = torch.empty(self.array_bytes + 256, dtype=torch.uint8, device=dev)
         self.dst = torch.empty_like(self.src)
-        tg.fill_random_u32(self.src, (ARRAY_BYTES + 256) // 4, seed=0)
+        tg.fill_random_u32(self.src, (self.array_bytes + 256) // 4, seed=0)
+        if self.array_bytes != ARRAY_BYTES:
+            self.config = dict(self.config, structs_per_width={str(s): n for s, _, n in self.plan},
+                               workload=self.config["workload"].replace("2 GiB", f"{args.array_mib} MiB"))
         self.written = {s: n for s, _, n in self.plan}
         self.tuned = {}
 
@@ -287,15 +293,16 @@ class Sweep:
 
     def kernel_bytes(self, key):
         w = int(key.rsplit("_", 1)[1][:-1])
-        s, n = w // 4, ARRAY_BYTES // w
+        s, n = w // 4, self.array_bytes // w
         return n * w + self.written[s] * w
 
     def e2e(self, world, steps):
         torch, tg = self.torch, self.tg
-        h_src = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
-        h_dst = torch.empty(ARRAY_BYTES, dtype=torch.uint8).pin_memory()
-        h_src.copy_(self.src[:ARRAY_BYTES].cpu())
-        tg.copy_host(h_dst, h_src, ARRAY_BYTES // 64, 64)  # warm the staging ring
+        ab = self.array_bytes
+        h_src = torch.empty(ab, dtype=torch.uint8).pin_memory()
+        h_dst = torch.empty(ab, dtype=torch.uint8).pin_memory()
+        h_src.copy_(self.src[:ab].cpu())
+        tg.copy_host(h_dst, h_src, ab // 64, 64)  # warm the staging ring
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -538,7 +545,107 @@ class Batch:
                 "batched_vs_per_call": round(self.per_call_ms / self._batch_ms, 3)}
 
 
-WORKLOADS = {"sweep": Sweep, "gather": Gather, "batch": Batch}
+SERVE_RATES = [2000, 5000, 10000, 20000, 50000]
+SERVE_WIDTHS = [8, 12, 16, 28, 64]
+SERVE_POOL = 1 << 23
+
+
+def serve_requests(rate, seconds, seed, src_ptr, idx_ptr):
+    """Seeded request stream: Poisson arrivals at `rate` per second for
+    `seconds`; 50 % copy / 50 % gather, width uniform from SERVE_WIDTHS,
+    length log-uniform in [256, 2^23] structs, sources and index windows at
+    random offsets of the device-resident pools."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    count = max(1, int(rate * seconds))
+    arrivals = np.cumsum(rng.exponential(1000.0 / rate, size=count))
+    ops = rng.integers(0, 2, size=count)
+    widths = rng.choice(SERVE_WIDTHS, size=count)
+    lens = np.exp(rng.uniform(math.log(256), math.log(SERVE_POOL), size=count)).astype(np.int64)
+    offs = (rng.random(size=count) * (SERVE_POOL - lens + 1)).astype(np.int64)
+    reqs = []
+    for k in range(count):
+        w, n, off = int(widths[k]), int(lens[k]), int(offs[k])
+        if ops[k] == 0:
+            reqs.append({"op": 0, "width": w, "n": n, "src": src_ptr[w] + off * w, "src_n": n})
+        else:
+            reqs.append({"op": 1, "width": w, "n": n, "src": src_ptr[w], "src_n": SERVE_POOL, "idx": idx_ptr + 4 * off})
+    return reqs, arrivals
+
+
+class Serve:
+    name = "serve"
+    config = {
+        "workload": "serving stream: Poisson arrivals at offered loads 2k-50k req/s, 50% copy / 50% gather, "
+                    "len log-uniform [256, 2^23] structs, width from {8,12,16,28,64} B, uniform int32 indices, "
+                    "device-resident sources, 64 GB HBM budget, continuous batching into the persistent kernel",
+        "offered_loads_per_s": SERVE_RATES, "seconds_per_load": 1.0, "budget_bytes": 64 << 30,
+        "max_inflight_batches": 4, "max_batch_requests": 1024,
+        "l2": "each load moves tens of GB, no flush",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        self.torch, self.tg, self.dev = torch, tg, dev
+        self.src = {}
+        for w in SERVE_WIDTHS:
+            t = torch.empty(SERVE_POOL * w, dtype=torch.uint8, device=dev)
+            tg.fill_random_u32(t, SERVE_POOL * w // 4, seed=w)
+            self.src[w] = t
+        self.idx = torch.empty(SERVE_POOL, dtype=torch.int32, device=dev)
+        tg.fill_uniform_indices(self.idx, SERVE_POOL, SERVE_POOL, seed=3)
+        self.ptrs = {w: t.data_ptr() for w, t in self.src.items()}
+        self.rows = []
+
+    def tune(self):
+        pass
+
+    def verify(self):
+        """300 requests served as a mixed stream must equal the same requests
+        run alone, byte for byte."""
+        torch, tg = self.torch, self.tg
+        reqs, arr = serve_requests(20000, 0.015, 99, self.ptrs, self.idx.data_ptr())
+        server = tg.Server(64 << 30, max_inflight=4, max_batch_requests=1024)
+        ids, _ = server.replay(reqs, arr)
+        for rid, r in zip(ids, reqs):
+            res = server.wait(rid)
+            n, w = r["n"], r["width"]
+            got = torch.empty(n * w, dtype=torch.uint8, device=self.dev)
+            tg.copy(got, res.dst, n, w)
+            ref = torch.empty_like(got)
+            if r["op"] == 0:
+                tg.copy(ref, r["src"], n, w)
+            else:
+                tg.gather(ref, r["src"], r["src_n"], r["idx"], n, w)
+            if not torch.equal(got, ref):
+                raise SystemExit("bench verification failed: served request differs from the same request alone")
+            server.release(rid)
+        server.close()
+
+    def run(self, seconds):
+        tg = self.tg
+        server = tg.Server(64 << 30, max_inflight=4, max_batch_requests=1024, release_when_done=True)
+        # warm-up stream (not reported)
+        reqs, arr = serve_requests(5000, 0.1, 1, self.ptrs, self.idx.data_ptr())
+        server.replay(reqs, arr)
+        total_bytes, total_ms = 0, 0.0
+        for k, rate in enumerate(SERVE_RATES):
+            reqs, arr = serve_requests(rate, seconds, 10 + k, self.ptrs, self.idx.data_ptr())
+            _, st = server.replay(reqs, arr)
+            span = st["last_done_ms"] - st["first_submit_ms"]
+            self.rows.append({"offered_per_s": rate, "requests": st["completed"],
+                              "achieved_per_s": round(st["completed"] / span * 1e3, 1),
+                              "gbs": round(st["bytes"] / span / 1e6, 1), "p50_ms": round(st["p50_ms"], 3),
+                              "p99_ms": round(st["p99_ms"], 3), "max_ms": round(st["max_ms"], 3),
+                              "max_queued": st["max_queued"]})
+            total_bytes += st["bytes"]
+            total_ms += span
+        stats = server.stats()
+        server.close()
+        return total_bytes, total_ms, stats
+
+
+WORKLOADS = {"sweep": Sweep, "gather": Gather, "batch": Batch, "serve": Serve}
 
 
 # ---- CPU baseline (the oracle's multithreaded port) ----------------------------
@@ -579,6 +686,30 @@ def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = 
                     done += (2 * w + 4) * n
             return done
         desc = "the 21 gathers on 2^21 structs (1/8 of the workload's length)"
+    elif workload == "serve":
+        pool = 1 << 20
+        srcs = {w: oracle.random_words(pool * w // 4, w, threads=threads).view(np.uint8) for w in SERVE_WIDTHS}
+        pidx = oracle.uniform_indices(pool, pool, 3)
+        rng = np.random.default_rng(10)
+        sample = []
+        for _ in range(200):
+            w = int(rng.choice(SERVE_WIDTHS))
+            n = int(np.exp(rng.uniform(math.log(256), math.log(pool))))
+            off = int(rng.integers(0, pool - n + 1))
+            sample.append((int(rng.integers(0, 2)), w, n, off))
+        dst = np.zeros(pool * 64, np.uint8)
+
+        def one():
+            done = 0
+            for op, w, n, off in sample:
+                if op == 0:
+                    oracle.run_mt(0, dst, srcs[w][off * w:], None, n, w, threads)
+                    done += 2 * n * w
+                else:
+                    oracle.run_mt(1, dst, srcs[w], pidx[off:], n, w, threads)
+                    done += 2 * n * w + 4 * n
+            return done
+        desc = "200 requests of the serving mix on 2^20-struct pools (lengths log-uniform up to 2^20)"
     else:
         rng = np.random.default_rng(4)
         ops = rng.choice([0, 1, 2], size=BATCH_COUNT, p=[0.5, 0.4, 0.1])
@@ -630,10 +761,56 @@ def run_reference(args, world, rank):
     }), flush=True)
 
 
+def run_serve(args, world, rank, local):
+    """The serving workload: one open-loop replay per offered load; the
+    reported value is the bytes of all completed requests over the time from
+    each stream's first submission to its last completion."""
+    import torch
+
+    import trove_gb300 as tg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    tg.load(build_if_missing=True)
+    load_tune_cache(tg, args.tune_cache)
+    wl = Serve(torch, tg, dev, args)
+    if not args.no_check:
+        wl.verify()
+    barrier(world)
+    clocks = Clocks(local)
+    total_bytes, total_ms, stats = wl.run(1.0)
+    clock_info = clocks.stop()
+    ms = reduce_max(total_ms, world, dev)
+    peak, peak_kind = hbm_peak()
+    value = total_bytes * world / (ms / 1e3) / 1e9
+    top = max(wl.rows, key=lambda r: r["gbs"])
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:
+        total, el, desc = cpu_sample("serve", os.cpu_count() or 1, args.cpu_seconds)
+        cpu = {"value": round(total / el / 1e9, 2), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": desc}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": len(SERVE_RATES),
+        "warmup": 1, "ms_per_step": round(ms / len(SERVE_RATES), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64 words)",
+        "config": Serve.config, "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak,
+        "peak_kind": peak_kind,
+        "roofline": {"bound": "hbm", "kernel": "batch_kernel (served)", "achieved": top["gbs"], "peak": peak,
+                     "unit": "GB/s", "frac": round(top["gbs"] / peak, 4), "traffic": None,
+                     "peak_kind": f"of {peak_kind}"},
+        "latency_by_load": wl.rows, "p99_ms": {str(r["offered_per_s"]): r["p99_ms"] for r in wl.rows},
+        "e2e": None, "gpu_launches": int(stats["batches"]), "clocks": clock_info, "cpu_baseline": cpu,
+        "details": {"server": stats},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_trove(args, world, rank, local):
     import torch
 
     import trove_gb300 as tg
+    if args.workload == "serve":
+        return run_serve(args, world, rank, local)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     tg.load(build_if_missing=True)

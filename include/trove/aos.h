@@ -13,8 +13,9 @@
 // time (uniform across the tile, so it costs one branch).  One-word structs
 // and structs of more words than the tile has lanes are read per lane.
 //
-// load(p) / store(v, p) take any pointers.  On a fully converged warp, one
-// __match_any_sync on p - lane tells whether the pointers are consecutive:
+// load(p) / store(v, p) take any pointers.  On a fully converged warp, a
+// broadcast of lane 0's pointer and one __ballot_sync tell whether the
+// pointers are consecutive:
 // if so the warp-contiguous path runs; if not, structs of 2..32 words move as
 // cooperative rounds (each struct read by adjacent lanes in one instruction)
 // plus a transpose, and one-word structs move per lane.  A partial warp moves
@@ -213,13 +214,15 @@ TROVE_D void warp_scatter_store(const T& data, T* dst) {
 }
 
 // For a fully converged warp: do lanes 0..31 address consecutive structs in
-// lane order?  Lanes agree on p - lane exactly when they do.
+// lane order?  Lane 0's address is broadcast and one __ballot_sync checks
+// every lane against it (cheaper than a match over 32 distinct addresses,
+// which the random case would pay on every access).
 template <typename T>
 TROVE_D bool warp_consecutive(const T* p) {
-    const unsigned long long key =
-        static_cast<unsigned long long>(reinterpret_cast<std::uintptr_t>(p)) -
-        static_cast<unsigned long long>(lane_id()) * sizeof(T);
-    return __match_any_sync(0xFFFFFFFFu, key) == 0xFFFFFFFFu;
+    const unsigned long long a = static_cast<unsigned long long>(reinterpret_cast<std::uintptr_t>(p));
+    const unsigned long long a0 = __shfl_sync(0xFFFFFFFFu, a, 0);
+    const bool mine = a == a0 + static_cast<unsigned long long>(lane_id()) * sizeof(T);
+    return __ballot_sync(0xFFFFFFFFu, mine) == 0xFFFFFFFFu;
 }
 
 }  // namespace detail

@@ -162,8 +162,9 @@ typedef struct trv_task {
 
 typedef struct trv_batch_options {
     int32_t tile_bytes;  /* payload bytes per tile; 0: autotuner cache, else the size rule */
-    int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO, TRV_PATH_VECTOR or TRV_PATH_WARP */
+    int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO or TRV_PATH_VECTOR (flat vector tiles) */
     int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
+    int32_t blocks_per_sm; /* 0 or 4: 64 registers per thread; 2: 128 registers (fewer, fatter warps) */
 } trv_batch_options;
 
 typedef struct trv_batch trv_batch;
@@ -187,6 +188,72 @@ int32_t trv_batch_destroy(trv_batch* batch);
  * trv_scatter, AUTO path), in order, on `stream`. */
 int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream);
 
+/* ---- serving -------------------------------------------------------------------
+ * A request loop for copy and gather requests against device-resident sources.
+ * Requests are admitted in arrival order while their output fits in the HBM
+ * budget (outputs live in one device arena of that size), folded into the
+ * batched persistent kernel as soon as a batch slot is free, and up to
+ * `max_inflight` batches run concurrently on separate streams, so requests that
+ * arrive while others are on the GPU join the next batch (continuous batching).
+ * A dispatcher thread owned by the server does admission, launch and
+ * completion.  No reference counterpart. */
+
+typedef struct trv_server_config {
+    uint64_t hbm_budget_bytes;   /* output arena size */
+    int32_t max_inflight;        /* concurrent batches (streams); 0: 4 */
+    int32_t max_batch_requests;  /* requests per batch; 0: 1024 */
+    int32_t tile_bytes;          /* 0: autotuner cache, else the size rule */
+    int32_t release_when_done;   /* 1: outputs are freed as soon as a request completes */
+} trv_server_config;
+
+typedef struct trv_request {
+    int32_t op;            /* TRV_OP_COPY or TRV_OP_GATHER */
+    uint32_t width;        /* bytes per struct: a multiple of 4, at most 64 */
+    uint64_t n;            /* structs produced */
+    const void* src;       /* device source (copy: n structs; gather: src_n structs) */
+    uint64_t src_n;        /* gather: source length */
+    const int32_t* idx;    /* gather: n device indices */
+} trv_request;
+
+typedef struct trv_result {
+    int32_t status;        /* TRV_OK when done; TRV_ERR_BUSY while queued or running */
+    int32_t batch;         /* sequence number of the batch that ran it */
+    void* dst;             /* device output (server-owned until released) */
+    double submit_ms;      /* host times, ms since the server started */
+    double launch_ms;
+    double done_ms;
+} trv_result;
+
+typedef struct trv_server_stats {
+    uint64_t submitted, admitted, completed, rejected, batches;
+    uint64_t max_queued;         /* most requests waiting for admission at once */
+    uint64_t bytes;              /* algorithmic bytes of completed requests */
+    uint64_t budget_in_use;      /* arena bytes held now */
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> done latency of completed requests */
+    double first_submit_ms, last_done_ms;
+} trv_server_stats;
+
+typedef struct trv_server trv_server;
+
+int32_t trv_server_create(const trv_server_config* cfg, trv_server** out);
+/* Queues a request; returns at once.  TRV_ERR_BUDGET if its output alone
+ * exceeds the budget. */
+int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id);
+/* TRV_OK with the result once done, TRV_ERR_BUSY before, TRV_ERR_NOT_FOUND
+ * for an unknown or released id. */
+int32_t trv_server_poll(trv_server* s, uint64_t id, trv_result* out);
+int32_t trv_server_wait(trv_server* s, uint64_t id, double timeout_ms, trv_result* out);
+/* Frees a completed request's output (its budget returns to the arena). */
+int32_t trv_server_release(trv_server* s, uint64_t id);
+int32_t trv_server_stats_get(trv_server* s, trv_server_stats* out);
+/* Open-loop load: submits reqs[k] when arrival_ms[k] (ms from the call) is
+ * reached, from a native thread, and returns when every request is done.
+ * ids (optional, count entries) receives the request ids. */
+int32_t trv_server_replay(trv_server* s, const trv_request* reqs, const double* arrival_ms, uint64_t count,
+                          uint64_t* ids, trv_server_stats* out);
+/* Drains outstanding work, then frees everything. */
+int32_t trv_server_destroy(trv_server* s);
+
 /* ---- autotuner -------------------------------------------------------------
  * Launch choices cached per (scope, op, width, length bucket of a factor 4).
  * Scope 0 (per call) steers the AUTO path of trv_copy / trv_gather /
@@ -198,9 +265,9 @@ int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream);
  * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625) and caches
  * the fastest in scope 0. */
 int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream);
-/* Times tile sizes (and copy variants) for each (op, width, bucket) group of
- * the given tasks, running each group alone as a batch, and caches the
- * fastest in scope 1.  The tasks' arrays are read and written. */
+/* Times tile sizes for each (op, width, bucket) group of the given tasks,
+ * running each group alone as a batch, and caches the fastest in scope 1.
+ * The tasks' arrays are read and written. */
 int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream);
 /* Cached choice for (scope, op, width, n); TRV_ERR_NOT_FOUND if none. */
 int32_t trv_autotune_lookup(int32_t scope, int32_t op, uint32_t width, uint64_t n, trv_launch* out,

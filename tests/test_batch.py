@@ -59,8 +59,9 @@ def test_batch_argument_errors(trove_lib):
         with pytest.raises(tg.TroveError) as e:
             tg.Batch(tasks)
         assert e.value.status == status
-    with pytest.raises(tg.TroveError):
-        tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path="bulk")
+    for bad_path in ["bulk", "warp"]:
+        with pytest.raises(tg.TroveError):
+            tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path=bad_path)
 
 
 def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000):
@@ -116,7 +117,7 @@ def check(tasks, expect):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("copy_path", ["vector", "warp", "auto"])
+@pytest.mark.parametrize("copy_path", ["vector", "auto"])
 @pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
 def test_batch_matches_oracle(cuda, copy_path, tile_bytes):
     torch = cuda

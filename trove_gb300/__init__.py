@@ -70,7 +70,8 @@ class Task(ctypes.Structure):
 
 
 class BatchOptions(ctypes.Structure):
-    _fields_ = [("tile_bytes", ctypes.c_int32), ("copy_path", ctypes.c_int32), ("grid_blocks", ctypes.c_int32)]
+    _fields_ = [("tile_bytes", ctypes.c_int32), ("copy_path", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32)]
 
 
 _lib = None
@@ -259,11 +260,11 @@ class Batch:
     """A planned batch (trv_batch): launch() runs every task in one
     persistent kernel; capture() records it as a CUDA graph first."""
 
-    def __init__(self, tasks, *, tile_bytes: int = 0, copy_path=PATH_AUTO, grid: int = 0):
+    def __init__(self, tasks, *, tile_bytes: int = 0, copy_path=PATH_AUTO, grid: int = 0, blocks_per_sm: int = 0):
         if isinstance(copy_path, str):
             copy_path = PATHS[copy_path]
         self._tasks = make_tasks(tasks)
-        opt = BatchOptions(int(tile_bytes), int(copy_path), int(grid))
+        opt = BatchOptions(int(tile_bytes), int(copy_path), int(grid), int(blocks_per_sm))
         h = ctypes.c_void_p()
         _check(load().trv_batch_create(self._tasks, len(self._tasks), ctypes.byref(opt), ctypes.byref(h)),
                "trv_batch_create")
@@ -329,3 +330,113 @@ def autotune_save(path):
 
 def autotune_load(path):
     _check(load().trv_autotune_load(str(path).encode()), "trv_autotune_load")
+
+
+# ---- serving ------------------------------------------------------------------------
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_int32),
+                ("max_batch_requests", ctypes.c_int32), ("tile_bytes", ctypes.c_int32),
+                ("release_when_done", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("width", ctypes.c_uint32), ("n", ctypes.c_uint64),
+                ("src", ctypes.c_void_p), ("src_n", ctypes.c_uint64), ("idx", ctypes.c_void_p)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("batch", ctypes.c_int32), ("dst", ctypes.c_void_p),
+                ("submit_ms", ctypes.c_double), ("launch_ms", ctypes.c_double), ("done_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "admitted", "completed", "rejected", "batches",
+                                               "max_queued", "bytes", "budget_in_use")] + \
+               [(k, ctypes.c_double) for k in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "first_submit_ms",
+                                               "last_done_ms")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_SIGNATURES.update({
+    "trv_server_create": (ctypes.c_int32, [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "trv_server_submit": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "trv_server_poll": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(Result)]),
+    "trv_server_wait": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(Result)]),
+    "trv_server_release": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64]),
+    "trv_server_stats_get": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "trv_server_replay": (ctypes.c_int32, [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.POINTER(ServerStats)]),
+    "trv_server_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
+})
+
+
+def make_request(r) -> Request:
+    if isinstance(r, Request):
+        return r
+    return Request(int(r["op"]), int(r["width"]), int(r["n"]), _addr(r["src"]), int(r.get("src_n", 0)),
+                   _addr(r.get("idx")))
+
+
+class Server:
+    """trv_server: admission against an HBM budget, continuous batching into
+    the persistent kernel, per-request latency."""
+
+    def __init__(self, budget_bytes: int, *, max_inflight: int = 0, max_batch_requests: int = 0,
+                 tile_bytes: int = 0, release_when_done: bool = False):
+        cfg = ServerConfig(int(budget_bytes), int(max_inflight), int(max_batch_requests), int(tile_bytes),
+                           1 if release_when_done else 0)
+        h = ctypes.c_void_p()
+        _check(load().trv_server_create(ctypes.byref(cfg), ctypes.byref(h)), "trv_server_create")
+        self._h = h
+
+    def submit(self, req) -> int:
+        rid = ctypes.c_uint64()
+        _check(load().trv_server_submit(self._h, ctypes.byref(make_request(req)), ctypes.byref(rid)),
+               "trv_server_submit")
+        return rid.value
+
+    def poll(self, rid: int):
+        res = Result()
+        rc = load().trv_server_poll(self._h, rid, ctypes.byref(res))
+        if rc == 9:
+            return None
+        _check(rc, "trv_server_poll")
+        return res
+
+    def wait(self, rid: int, timeout_ms: float = 60000.0) -> Result:
+        res = Result()
+        _check(load().trv_server_wait(self._h, rid, timeout_ms, ctypes.byref(res)), "trv_server_wait")
+        return res
+
+    def release(self, rid: int):
+        _check(load().trv_server_release(self._h, rid), "trv_server_release")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(load().trv_server_stats_get(self._h, ctypes.byref(st)), "trv_server_stats")
+        return st.as_dict()
+
+    def replay(self, requests, arrival_ms):
+        """Open-loop replay; returns (ids, stats dict) for these requests."""
+        n = len(requests)
+        arr = (Request * n)(*[make_request(r) for r in requests])
+        times = (ctypes.c_double * n)(*[float(t) for t in arrival_ms])
+        ids = (ctypes.c_uint64 * n)()
+        st = ServerStats()
+        _check(load().trv_server_replay(self._h, arr, times, n, ids, ctypes.byref(st)), "trv_server_replay")
+        return list(ids), st.as_dict()
+
+    def close(self):
+        if self._h:
+            h, self._h = self._h, None
+            _check(load().trv_server_destroy(h), "trv_server_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

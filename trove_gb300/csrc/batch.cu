@@ -30,9 +30,19 @@ constexpr int kWarps = kBatchBlock / 32;
 
 // ---- per-tile movers (all warps of the CTA cooperate on one tile) --------
 
+// Thread position read through volatile asm: the movers' lane-derived
+// constants are then recomputed per tile instead of being hoisted out of the
+// persistent loop for every (op, width) case at once, which would keep
+// hundreds of them live and spill.
+__device__ __forceinline__ int opaque_tid() {
+    int t;
+    asm volatile("mov.u32 %0, %%tid.x;" : "=r"(t));
+    return t;
+}
+
 // Flat copy of a byte range with the widest vector both pointers allow.
 __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned char* d, long long nbytes) {
-    const int tid = threadIdx.x;
+    const int tid = opaque_tid();
     const unsigned a = unsigned(reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d));
     long long done = 0;
     if ((a & 15u) == 0) {
@@ -59,111 +69,79 @@ __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned 
     for (long long b = done + tid; b < nbytes; b += kBatchBlock) d[b] = s[b];
 }
 
-// Device-API copy of structs [first, first + cnt): full 32-struct chunks with
-// load/store_warp_contiguous, the ragged end per lane.
-template <int S>
-__device__ __forceinline__ void tile_copy_warp(const aos<S>* src, aos<S>* dst, long long first, long long cnt) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long end = first + cnt;
-    for (long long base = first + warp * 32; base < end; base += kWarps * 32) {
-        const long long i = base + lane;
-        if (base + 32 <= end) {
-            const aos<S> v = trove::load_warp_contiguous(src + i);
-            trove::store_warp_contiguous(v, dst + i);
-        } else if (i < end) {
-            trove::detail::divergent_store(trove::detail::divergent_load(src + i), dst + i);
-        }
-    }
-}
-
 // Row-form gather / scatter over outputs (gather) or inputs (scatter)
-// [first, first + cnt), words of V, U chunks of 32 per warp pass.
-template <int S, typename V, int U, bool GATHER>
+// [first, first + cnt) in words of V, m words per struct given at run time
+// (so one mover serves every width).  Each warp pass moves U chunks of 32
+// structs; a chunk's m rounds run in groups of G (loads of the group, then its
+// stores).  Round k, lane l: word q = l + 32k of the chunk, i.e. word q % m of
+// struct q / m, whose index comes from that struct's lane by one shuffle.  m is
+// uniform across the warp, so the guarded shuffles are too.
+template <typename V, int U, int G, bool GATHER>
 __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int* idx, long long bound, long long first,
-                                                long long cnt) {
-    constexpr int m = S * 4 / int(sizeof(V));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                                                long long cnt, int m) {
+    const int tid = opaque_tid();
+    const int lane = tid & 31, warp = tid >> 5;
     const long long end = first + cnt;
     for (long long base = first + warp * 32 * U; base < end; base += kWarps * 32 * U) {
         int id[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const long long i = base + u * 32 + lane;
-            const int v = i < end ? __ldg(idx + i) : -1;
+            const int v = i < end ? __ldcs(idx + i) : -1;
             id[u] = (v >= 0 && (long long)v < bound) ? v : -1;
         }
-        V val[U][m];
-        int other[U][m];
+        for (int k0 = 0; k0 < m; k0 += G) {
+            V val[U][G];
+            int other[U][G];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
+            for (int u = 0; u < U; ++u)
 #pragma unroll
-            for (int k = 0; k < m; ++k) {
-                const int q = lane + 32 * k;
-                const int j = q / m;
-                other[u][k] = __shfl_sync(0xFFFFFFFFu, id[u], j);
-                if (other[u][k] >= 0)
-                    val[u][k] = GATHER ? __ldg(src + (long long)other[u][k] * m + (q - j * m))
-                                       : __ldg(src + (base + u * 32) * m + q);
-            }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-#pragma unroll
-            for (int k = 0; k < m; ++k) {
-                const int q = lane + 32 * k;
-                if (other[u][k] >= 0) {
-                    if (GATHER)
-                        dst[(base + u * 32) * m + q] = val[u][k];
-                    else
-                        dst[(long long)other[u][k] * m + (q - (q / m) * m)] = val[u][k];
+                for (int g = 0; g < G; ++g) {
+                    const int k = k0 + g;
+                    other[u][g] = -1;
+                    if (k < m) {
+                        const int q = lane + 32 * k;
+                        const int j = q / m;
+                        other[u][g] = __shfl_sync(0xFFFFFFFFu, id[u], j);
+                        if (other[u][g] >= 0)
+                            val[u][g] = GATHER ? __ldg(src + (long long)other[u][g] * m + (q - j * m))
+                                               : __ldcs(src + (base + u * 32) * m + q);
+                    }
                 }
-            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (other[u][g] < 0) continue;
+                    const int q = lane + 32 * (k0 + g);
+                    if (GATHER)
+                        __stcs(dst + (base + u * 32) * m + q, val[u][g]);
+                    else
+                        dst[(long long)other[u][g] * m + (q % m)] = val[u][g];
+                }
+        }
     }
 }
 
-// Unroll for the index movers: about 8 words of payload in flight per lane.
-template <int S, typename V>
-struct batch_unroll {
-    static constexpr int m = S * 4 / int(sizeof(V));
-    static constexpr int value = m >= 8 ? 1 : (m >= 4 ? 2 : (m >= 2 ? 4 : 8));
-};
-
-template <int S, bool GATHER>
+template <bool GATHER>
 __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, long long cnt) {
-    constexpr int wide = (S % 4 == 0) ? 16 : (S % 2 == 0) ? 8 : 4;
-    const unsigned a = unsigned(reinterpret_cast<uintptr_t>(t.src) | reinterpret_cast<uintptr_t>(t.dst));
-    if constexpr (wide == 16) {
-        if ((a & 15u) == 0) {
-            tile_index_rows<S, uint4, batch_unroll<S, uint4>::value, GATHER>(
-                reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst), t.idx, t.bound, first, cnt);
-            return;
-        }
-    }
-    if constexpr (wide >= 8) {
-        if ((a & 7u) == 0) {
-            tile_index_rows<S, uint2, batch_unroll<S, uint2>::value, GATHER>(
-                reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst), t.idx, t.bound, first, cnt);
-            return;
-        }
-    }
-    tile_index_rows<S, unsigned, batch_unroll<S, unsigned>::value, GATHER>(
-        reinterpret_cast<const unsigned*>(t.src), reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt);
+    const int m = t.words * 4 >> t.word_log2;
+    if (t.word_log2 == 4)
+        tile_index_rows<uint4, 2, 2, GATHER>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
+                                             t.idx, t.bound, first, cnt, m);
+    else if (t.word_log2 == 3)
+        tile_index_rows<uint2, 2, 4, GATHER>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
+                                             t.idx, t.bound, first, cnt, m);
+    else
+        tile_index_rows<unsigned, 2, 4, GATHER>(reinterpret_cast<const unsigned*>(t.src),
+                                                reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m);
 }
 
-template <int S>
-__device__ __forceinline__ void run_tile(const BatchTask& t, long long first, long long cnt) {
-    if (t.op == TRV_OP_COPY) {
-        if (t.variant == TRV_PATH_WARP)
-            tile_copy_warp<S>(reinterpret_cast<const aos<S>*>(t.src), reinterpret_cast<aos<S>*>(t.dst), first, cnt);
-        else
-            tile_copy_flat(t.src + first * 4 * S, t.dst + first * 4 * S, cnt * 4 * S);
-    } else if (t.op == TRV_OP_GATHER) {
-        tile_index<S, true>(t, first, cnt);
-    } else {
-        tile_index<S, false>(t, first, cnt);
-    }
-}
-
-__global__ void __launch_bounds__(kBatchBlock)
+// MINB resident blocks per SM: 2 gives each thread 128 registers (no
+// spills), 4 gives 64 (a few spilled words, twice the warps for latency
+// hiding); the batch options or the autotuner pick one.
+template <int MINB>
+__global__ void __launch_bounds__(kBatchBlock, MINB)
 batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* __restrict__ tile_prefix,
              unsigned long long* counter) {
     __shared__ long long s_tile;
@@ -185,34 +163,28 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
         const BatchTask& t = tasks[lo];
         const long long first = (tile - __ldg(tile_prefix + lo)) * t.tile_structs;
         const long long cnt = t.n - first < t.tile_structs ? t.n - first : t.tile_structs;
-        switch (t.words) {
-            case 1: run_tile<1>(t, first, cnt); break;
-            case 2: run_tile<2>(t, first, cnt); break;
-            case 3: run_tile<3>(t, first, cnt); break;
-            case 4: run_tile<4>(t, first, cnt); break;
-            case 5: run_tile<5>(t, first, cnt); break;
-            case 6: run_tile<6>(t, first, cnt); break;
-            case 7: run_tile<7>(t, first, cnt); break;
-            case 8: run_tile<8>(t, first, cnt); break;
-            case 9: run_tile<9>(t, first, cnt); break;
-            case 10: run_tile<10>(t, first, cnt); break;
-            case 11: run_tile<11>(t, first, cnt); break;
-            case 12: run_tile<12>(t, first, cnt); break;
-            case 13: run_tile<13>(t, first, cnt); break;
-            case 14: run_tile<14>(t, first, cnt); break;
-            case 15: run_tile<15>(t, first, cnt); break;
-            case 16: run_tile<16>(t, first, cnt); break;
-        }
+        const long long w = 4ll * t.words;
+        if (t.op == TRV_OP_COPY)
+            tile_copy_flat(t.src + first * w, t.dst + first * w, cnt * w);
+        else if (t.op == TRV_OP_GATHER)
+            tile_index<true>(t, first, cnt);
+        else
+            tile_index<false>(t, first, cnt);
     }
 }
 
 }  // namespace
 
-const void* batch_kernel_func() { return (const void*)&batch_kernel; }
+const void* batch_kernel_func(int blocks_per_sm) {
+    return blocks_per_sm == 2 ? (const void*)&batch_kernel<2> : (const void*)&batch_kernel<4>;
+}
 
 cudaError_t launch_batch_kernel(const BatchTask* tasks, int ntasks, const long long* tile_prefix,
-                                unsigned long long* counter, int grid, cudaStream_t st) {
-    batch_kernel<<<grid, kBatchBlock, 0, st>>>(tasks, ntasks, tile_prefix, counter);
+                                unsigned long long* counter, int grid, int blocks_per_sm, cudaStream_t st) {
+    if (blocks_per_sm == 2)
+        batch_kernel<2><<<grid, kBatchBlock, 0, st>>>(tasks, ntasks, tile_prefix, counter);
+    else
+        batch_kernel<4><<<grid, kBatchBlock, 0, st>>>(tasks, ntasks, tile_prefix, counter);
     return cudaGetLastError();
 }
 

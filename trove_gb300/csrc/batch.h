@@ -15,12 +15,13 @@ struct alignas(16) BatchTask {
     int op;           // TRV_OP_*
     int words;        // struct width / 4
     int tile_structs; // structs per tile, a multiple of 32
-    int variant;      // copy tasks: TRV_PATH_VECTOR or TRV_PATH_WARP
+    int word_log2;    // gather / scatter: log2 of the word moved per lane (2, 3 or 4)
 };
 
-const void* batch_kernel_func();
+// blocks_per_sm: 2 or 4 (the register budget the kernel was built for).
+const void* batch_kernel_func(int blocks_per_sm);
 cudaError_t launch_batch_kernel(const BatchTask* tasks, int ntasks, const long long* tile_prefix,
-                                unsigned long long* counter, int grid, cudaStream_t st);
+                                unsigned long long* counter, int grid, int blocks_per_sm, cudaStream_t st);
 int batch_block_threads();
 
 }  // namespace trv

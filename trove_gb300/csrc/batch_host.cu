@@ -21,6 +21,7 @@ struct trv_batch {
     long long total_tiles = 0;
     uint64_t bytes = 0;
     int grid = 0;
+    int blocks_per_sm = 4;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -42,6 +43,15 @@ int validate(const trv_task& t) {
         if (!aligned4(t.idx)) return TRV_ERR_MISALIGNED;
     }
     return TRV_OK;
+}
+
+// Word moved per lane by the row-form index movers: the widest of 16 / 8 / 4
+// bytes that divides the width and that both arrays are aligned to.
+int batch_word_log2(const trv_task& t) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(t.src) | reinterpret_cast<uintptr_t>(t.dst);
+    if (t.width % 16 == 0 && (a & 15u) == 0) return 4;
+    if (t.width % 8 == 0 && (a & 7u) == 0) return 3;
+    return 2;
 }
 
 // Size rule when no tuned tile exists: big enough to amortise the queue
@@ -72,13 +82,14 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     *out = nullptr;
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
     if (count >= uint64_t(INT_MAX)) return TRV_ERR_INVALID_ARGUMENT;
-    if (opt && opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR &&
-        opt->copy_path != TRV_PATH_WARP)
-        return TRV_ERR_UNSUPPORTED;
+    if (opt && opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR) return TRV_ERR_UNSUPPORTED;
     if (opt && opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
+    if (opt && opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4)
+        return TRV_ERR_UNSUPPORTED;
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
     uint64_t bytes = 0;
+    uint64_t vote2 = 0, vote4 = 0;  // bytes of tasks whose tuned entry prefers 2 / 4 blocks per SM
     for (uint64_t k = 0; k < count; ++k) {
         const trv_task& t = tasks[k];
         const int rc = validate(t);
@@ -92,9 +103,6 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         long long tile = (long long)tile_bytes / t.width;
         tile = tile < 32 ? 32 : (tile / 32) * 32;
         if (tile > (1 << 30)) tile = 1 << 30;
-        int variant = (opt && opt->copy_path != TRV_PATH_AUTO) ? opt->copy_path
-                      : (tuned && c.path != 0)                  ? c.path
-                                                                : TRV_PATH_VECTOR;
         BatchTask& d = host[k];
         d.src = static_cast<const unsigned char*>(t.src);
         d.dst = static_cast<unsigned char*>(t.dst);
@@ -104,9 +112,12 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         d.op = t.op;
         d.words = int(t.width / 4);
         d.tile_structs = int(tile);
-        d.variant = variant;
+        d.word_log2 = batch_word_log2(t);
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
-        bytes += 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
+        const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
+        bytes += tb;
+        if (tuned && c.grid == 2) vote2 += tb;
+        if (tuned && c.grid == 4) vote4 += tb;
     }
     trv_batch* b = new (std::nothrow) trv_batch;
     if (!b) return TRV_ERR_OUT_OF_MEMORY;
@@ -127,7 +138,10 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         cudaGetLastError();
         return e == cudaErrorMemoryAllocation ? TRV_ERR_OUT_OF_MEMORY : cuda_fail(e);
     }
-    const int resident = resident_blocks(batch_kernel_func(), batch_block_threads());
+    // One register budget for the whole kernel: the caller's, else the one the
+    // autotuner preferred for most of the batch's bytes, else 4 blocks per SM.
+    b->blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote2 > vote4 ? 2 : 4);
+    const int resident = resident_blocks(batch_kernel_func(b->blocks_per_sm), batch_block_threads());
     b->grid = (opt && opt->grid_blocks > 0) ? opt->grid_blocks : resident;
     if (b->total_tiles < b->grid) b->grid = b->total_tiles > 0 ? int(b->total_tiles) : 1;
     *out = b;
@@ -144,7 +158,7 @@ int32_t trv_batch_launch(trv_batch* b, void* stream) {
     if (b->total_tiles == 0) return TRV_OK;
     cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_fail(e);
-    e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, st);
+    e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, b->blocks_per_sm, st);
     return e == cudaSuccess ? TRV_OK : cuda_fail(e);
 }
 
@@ -162,7 +176,7 @@ int32_t trv_batch_capture(trv_batch* b, void* stream) {
     int rc = TRV_OK;
     if (b->total_tiles > 0) {
         e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), st);
-        if (e == cudaSuccess) e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, st);
+        if (e == cudaSuccess) e = launch_batch_kernel(b->d_tasks, b->ntasks, b->d_prefix, b->d_counter, b->grid, b->blocks_per_sm, st);
         if (e != cudaSuccess) rc = cuda_fail(e);
     }
     cudaGraph_t g = nullptr;

@@ -1,0 +1,505 @@
+// Serving: a request loop that admits copy / gather requests against an HBM
+// budget and folds them into the batched persistent kernel (batch.cu).
+//
+// One dispatcher thread per server repeats:
+//   1. completion — every in-flight batch whose event has fired marks its
+//      requests done (latency = submit -> observed completion);
+//   2. admission — queued requests, in arrival order, get their output carved
+//      from the budget arena (first fit, 256-byte granules) while it fits;
+//   3. launch — while a batch slot is free, up to max_batch_requests admitted
+//      requests become one batch: its task table and tile prefix are written
+//      to the slot's pinned staging, copied to the slot's device table, and
+//      the persistent kernel runs on the slot's stream.
+// With several slots, batches overlap on the GPU and requests that arrive
+// while others run join the next batch: continuous batching, not a queue in
+// front of a single launch.  Sources and index arrays stay device-resident
+// (the caller owns them); the server owns only outputs and its tables.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "autotune.h"
+#include "batch.h"
+#include "runtime.h"
+#include "trove_gb300.h"
+
+namespace trv {
+namespace {
+
+using clock_type = std::chrono::steady_clock;
+
+constexpr uint64_t kGranule = 256;
+
+// First-fit allocator over one device allocation.
+class Arena {
+public:
+    bool init(uint64_t bytes) {
+        size_ = (bytes + kGranule - 1) / kGranule * kGranule;
+        if (size_ == 0) return false;
+        if (cudaMalloc(&base_, size_) != cudaSuccess) {
+            cudaGetLastError();
+            base_ = nullptr;
+            return false;
+        }
+        free_[0] = size_;
+        return true;
+    }
+    ~Arena() {
+        if (base_) cudaFree(base_);
+    }
+    // Offset of a block of `bytes`, or UINT64_MAX if none fits.
+    uint64_t alloc(uint64_t bytes) {
+        bytes = (bytes + kGranule - 1) / kGranule * kGranule;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                const uint64_t off = it->first, left = it->second - bytes;
+                free_.erase(it);
+                if (left) free_[off + bytes] = left;
+                used_ += bytes;
+                return off;
+            }
+        }
+        return UINT64_MAX;
+    }
+    void release(uint64_t off, uint64_t bytes) {
+        bytes = (bytes + kGranule - 1) / kGranule * kGranule;
+        used_ -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    unsigned char* base() const { return static_cast<unsigned char*>(base_); }
+    uint64_t size() const { return size_; }
+    uint64_t used() const { return used_; }
+
+private:
+    void* base_ = nullptr;
+    uint64_t size_ = 0, used_ = 0;
+    std::map<uint64_t, uint64_t> free_;
+};
+
+enum ReqPhase { QUEUED, ADMITTED, LAUNCHED, DONE };
+
+struct Req {
+    trv_request r;
+    ReqPhase phase = QUEUED;
+    bool released = false;
+    uint64_t off = 0, bytes = 0;
+    int batch = -1;
+    double submit_ms = 0, launch_ms = 0, done_ms = 0;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    BatchTask* d_tasks = nullptr;
+    long long* d_prefix = nullptr;
+    unsigned long long* d_counter = nullptr;
+    BatchTask* h_tasks = nullptr;  // pinned staging
+    long long* h_prefix = nullptr;
+    std::vector<uint64_t> ids;
+    bool busy = false;
+};
+
+uint64_t request_bytes(const trv_request& r) {
+    return 2 * r.n * r.width + (r.op == TRV_OP_GATHER ? 4 * r.n : 0);
+}
+
+}  // namespace
+}  // namespace trv
+
+using namespace trv;
+
+struct trv_server {
+    trv_server_config cfg{};
+    int device = 0;
+    int grid = 1;
+    Arena arena;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable wake, finished;
+    std::deque<uint64_t> queue;
+    std::deque<uint64_t> admitted;
+    std::unordered_map<uint64_t, Req> reqs;
+    uint64_t next_id = 1;
+    int batches = 0;
+    bool stop = false;
+    int error = TRV_OK;
+    trv_server_stats st{};
+    std::vector<double> latencies;
+    clock_type::time_point t0 = clock_type::now();
+    std::thread dispatcher;
+
+    double now_ms() const {
+        return std::chrono::duration<double, std::milli>(clock_type::now() - t0).count();
+    }
+
+    void complete_ready() {  // lock held
+        for (Slot& s : slots) {
+            if (!s.busy) continue;
+            const cudaError_t q = cudaEventQuery(s.done);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess && error == TRV_OK) error = cuda_fail(q);
+            const double t = now_ms();
+            for (uint64_t id : s.ids) {
+                Req& r = reqs[id];
+                r.phase = DONE;
+                r.done_ms = t;
+                ++st.completed;
+                st.bytes += request_bytes(r.r);
+                latencies.push_back(r.done_ms - r.submit_ms);
+                if (cfg.release_when_done && !r.released) {
+                    arena.release(r.off, r.bytes);
+                    r.released = true;
+                }
+            }
+            s.ids.clear();
+            s.busy = false;
+            finished.notify_all();
+        }
+    }
+
+    void admit() {  // lock held
+        while (!queue.empty()) {
+            Req& r = reqs[queue.front()];
+            const uint64_t off = arena.alloc(r.bytes);
+            if (off == UINT64_MAX) break;  // FIFO: wait for budget to free up
+            r.off = off;
+            r.phase = ADMITTED;
+            admitted.push_back(queue.front());
+            queue.pop_front();
+            ++st.admitted;
+        }
+    }
+
+    void launch_ready() {  // lock held
+        for (Slot& s : slots) {
+            if (admitted.empty()) return;
+            if (s.busy) continue;
+            const size_t take = std::min<size_t>(admitted.size(), size_t(cfg.max_batch_requests));
+            s.ids.assign(admitted.begin(), admitted.begin() + take);
+            admitted.erase(admitted.begin(), admitted.begin() + take);
+            long long tiles = 0;
+            const double t = now_ms();
+            for (size_t k = 0; k < take; ++k) {
+                Req& r = reqs[s.ids[k]];
+                TuneChoice c;
+                const bool tuned = tune_lookup(TuneKey{SCOPE_BATCH, r.r.op, int(r.r.width), len_bucket(r.r.n)}, &c);
+                const int tb = cfg.tile_bytes > 0 ? cfg.tile_bytes
+                               : (tuned && c.tile_bytes > 0) ? c.tile_bytes
+                                                             : (r.r.op == TRV_OP_COPY ? (128 << 10) : (64 << 10));
+                long long tile = (long long)tb / r.r.width;
+                tile = tile < 32 ? 32 : (tile / 32) * 32;
+                BatchTask& d = s.h_tasks[k];
+                d.src = static_cast<const unsigned char*>(r.r.src);
+                d.dst = arena.base() + r.off;
+                d.idx = r.r.idx;
+                d.n = (long long)r.r.n;
+                d.bound = (long long)r.r.src_n;
+                d.op = r.r.op;
+                d.words = int(r.r.width / 4);
+                d.tile_structs = int(tile);
+                const uintptr_t al = reinterpret_cast<uintptr_t>(d.src) | reinterpret_cast<uintptr_t>(d.dst);
+                d.word_log2 = (r.r.width % 16 == 0 && (al & 15u) == 0) ? 4
+                              : (r.r.width % 8 == 0 && (al & 7u) == 0) ? 3
+                                                                        : 2;
+                s.h_prefix[k] = tiles;
+                tiles += (d.n + tile - 1) / tile;
+                r.phase = LAUNCHED;
+                r.batch = batches;
+                r.launch_ms = t;
+            }
+            s.h_prefix[take] = tiles;
+            cudaError_t e = cudaMemcpyAsync(s.d_tasks, s.h_tasks, sizeof(BatchTask) * take, cudaMemcpyHostToDevice,
+                                            s.stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(s.d_prefix, s.h_prefix, sizeof(long long) * (take + 1), cudaMemcpyHostToDevice,
+                                    s.stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), s.stream);
+            if (e == cudaSuccess) {
+                const int g = tiles < grid ? int(tiles > 0 ? tiles : 1) : grid;
+                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, 4, s.stream);
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
+            if (e != cudaSuccess && error == TRV_OK) error = cuda_fail(e);
+            s.busy = true;
+            ++batches;
+            ++st.batches;
+        }
+    }
+
+    bool any_busy() const {
+        for (const Slot& s : slots)
+            if (s.busy) return true;
+        return false;
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            complete_ready();
+            admit();
+            launch_ready();
+            if (stop && queue.empty() && admitted.empty() && !any_busy()) break;
+            if (any_busy()) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                lk.lock();
+            } else {
+                wake.wait_for(lk, std::chrono::milliseconds(1));
+            }
+        }
+    }
+};
+
+namespace {
+
+void free_slot(Slot& s) {
+    if (s.stream) cudaStreamDestroy(s.stream);
+    if (s.done) cudaEventDestroy(s.done);
+    if (s.d_tasks) cudaFree(s.d_tasks);
+    if (s.d_prefix) cudaFree(s.d_prefix);
+    if (s.d_counter) cudaFree(s.d_counter);
+    if (s.h_tasks) cudaFreeHost(s.h_tasks);
+    if (s.h_prefix) cudaFreeHost(s.h_prefix);
+    s = Slot();
+}
+
+int validate_request(const trv_request& r, uint64_t budget) {
+    if (r.op != TRV_OP_COPY && r.op != TRV_OP_GATHER) return TRV_ERR_INVALID_ARGUMENT;
+    if (r.width == 0 || r.n == 0 || r.n > (uint64_t(1) << 40) / r.width) return TRV_ERR_INVALID_ARGUMENT;
+    if (r.width % 4 != 0 || r.width > 64) return TRV_ERR_UNSUPPORTED;
+    if (!r.src || (reinterpret_cast<uintptr_t>(r.src) & 3u)) return TRV_ERR_INVALID_ARGUMENT;
+    if (r.op == TRV_OP_GATHER && (!r.idx || (reinterpret_cast<uintptr_t>(r.idx) & 3u) || r.src_n == 0))
+        return TRV_ERR_INVALID_ARGUMENT;
+    if (r.n * r.width > budget) return TRV_ERR_BUDGET;
+    return TRV_OK;
+}
+
+void fill_stats(const std::vector<double>& lat, trv_server_stats* out) {
+    if (lat.empty()) return;
+    std::vector<double> v(lat);
+    std::sort(v.begin(), v.end());
+    auto q = [&](double p) { return v[std::min(v.size() - 1, size_t(p * double(v.size() - 1) + 0.5))]; };
+    out->p50_ms = q(0.50);
+    out->p99_ms = q(0.99);
+    out->max_ms = v.back();
+    double sum = 0;
+    for (double x : v) sum += x;
+    out->mean_ms = sum / double(v.size());
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
+    if (!cfg || !out) return TRV_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_batch_requests < 0 || cfg->tile_bytes < 0)
+        return TRV_ERR_INVALID_ARGUMENT;
+    trv_server* s = new (std::nothrow) trv_server;
+    if (!s) return TRV_ERR_OUT_OF_MEMORY;
+    s->cfg = *cfg;
+    if (s->cfg.max_inflight == 0) s->cfg.max_inflight = 4;
+    if (s->cfg.max_batch_requests == 0) s->cfg.max_batch_requests = 1024;
+    cudaGetDevice(&s->device);
+    if (!s->arena.init(cfg->hbm_budget_bytes)) {
+        delete s;
+        return TRV_ERR_OUT_OF_MEMORY;
+    }
+    s->slots.resize(size_t(s->cfg.max_inflight));
+    const size_t nt = size_t(s->cfg.max_batch_requests);
+    for (Slot& sl : s->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_tasks, sizeof(BatchTask) * nt);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_prefix, sizeof(long long) * (nt + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_counter, sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tasks, sizeof(BatchTask) * nt);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_prefix, sizeof(long long) * (nt + 1));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            for (Slot& x : s->slots) free_slot(x);
+            delete s;
+            return e == cudaErrorMemoryAllocation ? TRV_ERR_OUT_OF_MEMORY : cuda_fail(e);
+        }
+    }
+    // Concurrent batches share the GPU: each gets an equal part of it.
+    const int resident = resident_blocks(batch_kernel_func(4), batch_block_threads());
+    s->grid = std::max(1, resident / s->cfg.max_inflight);
+    s->t0 = clock_type::now();
+    s->dispatcher = std::thread([s] { s->run(); });
+    *out = s;
+    return TRV_OK;
+}
+
+int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id) {
+    if (!s || !req) return TRV_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    ++s->st.submitted;
+    const int rc = validate_request(*req, s->arena.size());
+    if (rc != TRV_OK) {
+        ++s->st.rejected;
+        return rc;
+    }
+    if (s->stop) return TRV_ERR_CANCELLED;
+    const uint64_t k = s->next_id++;
+    Req& r = s->reqs[k];
+    r.r = *req;
+    r.bytes = req->n * req->width;
+    r.submit_ms = s->now_ms();
+    if (s->st.first_submit_ms == 0 && s->st.submitted == 1) s->st.first_submit_ms = r.submit_ms;
+    s->queue.push_back(k);
+    if (s->queue.size() > s->st.max_queued) s->st.max_queued = s->queue.size();
+    if (id) *id = k;
+    s->wake.notify_one();
+    return TRV_OK;
+}
+
+static void result_of(trv_server* s, const Req& r, trv_result* out) {
+    out->status = r.phase == DONE ? TRV_OK : TRV_ERR_BUSY;
+    out->batch = r.batch;
+    out->dst = r.phase >= ADMITTED ? s->arena.base() + r.off : nullptr;
+    out->submit_ms = r.submit_ms;
+    out->launch_ms = r.launch_ms;
+    out->done_ms = r.done_ms;
+}
+
+int32_t trv_server_poll(trv_server* s, uint64_t id, trv_result* out) {
+    if (!s) return TRV_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->error != TRV_OK) return s->error;
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || (it->second.released && !s->cfg.release_when_done)) return TRV_ERR_NOT_FOUND;
+    if (out) result_of(s, it->second, out);
+    return it->second.phase == DONE ? TRV_OK : TRV_ERR_BUSY;
+}
+
+int32_t trv_server_wait(trv_server* s, uint64_t id, double timeout_ms, trv_result* out) {
+    if (!s) return TRV_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto deadline = clock_type::now() + std::chrono::microseconds(int64_t(timeout_ms * 1000.0));
+    for (;;) {
+        if (s->error != TRV_OK) return s->error;
+        auto it = s->reqs.find(id);
+        if (it == s->reqs.end()) return TRV_ERR_NOT_FOUND;
+        if (it->second.phase == DONE) {
+            if (out) result_of(s, it->second, out);
+            return TRV_OK;
+        }
+        if (s->finished.wait_until(lk, deadline) == std::cv_status::timeout) {
+            it = s->reqs.find(id);
+            if (it != s->reqs.end() && it->second.phase == DONE) continue;
+            return TRV_ERR_TIMEOUT;
+        }
+    }
+}
+
+int32_t trv_server_release(trv_server* s, uint64_t id) {
+    if (!s) return TRV_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return TRV_ERR_NOT_FOUND;
+    Req& r = it->second;
+    if (r.phase != DONE) return TRV_ERR_BUSY;
+    if (!r.released) s->arena.release(r.off, r.bytes);
+    s->reqs.erase(it);
+    s->wake.notify_one();
+    return TRV_OK;
+}
+
+int32_t trv_server_stats_get(trv_server* s, trv_server_stats* out) {
+    if (!s || !out) return TRV_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(s->mu);
+    *out = s->st;
+    out->budget_in_use = s->arena.used();
+    fill_stats(s->latencies, out);
+    return s->error;
+}
+
+int32_t trv_server_replay(trv_server* s, const trv_request* reqs, const double* arrival_ms, uint64_t count,
+                          uint64_t* ids, trv_server_stats* out) {
+    if (!s || (count && (!reqs || !arrival_ms))) return TRV_ERR_INVALID_ARGUMENT;
+    std::vector<uint64_t> mine(count, 0);
+    const auto start = clock_type::now();
+    for (uint64_t k = 0; k < count; ++k) {
+        const auto when = start + std::chrono::nanoseconds(int64_t(arrival_ms[k] * 1e6));
+        if (clock_type::now() + std::chrono::microseconds(200) < when)
+            std::this_thread::sleep_until(when - std::chrono::microseconds(100));
+        while (clock_type::now() < when) {
+        }
+        const int rc = trv_server_submit(s, &reqs[k], &mine[k]);
+        if (rc != TRV_OK) return rc;
+    }
+    std::unique_lock<std::mutex> lk(s->mu);
+    trv_server_stats r{};
+    std::vector<double> lat;
+    lat.reserve(count);
+    for (uint64_t k = 0; k < count; ++k) {
+        for (;;) {
+            if (s->error != TRV_OK) return s->error;
+            auto it = s->reqs.find(mine[k]);
+            if (it == s->reqs.end() || it->second.phase == DONE) break;
+            s->finished.wait_for(lk, std::chrono::milliseconds(50));
+        }
+        auto it = s->reqs.find(mine[k]);
+        if (it == s->reqs.end()) continue;
+        const Req& q = it->second;
+        lat.push_back(q.done_ms - q.submit_ms);
+        r.bytes += request_bytes(q.r);
+        r.first_submit_ms = k == 0 ? q.submit_ms : std::min(r.first_submit_ms, q.submit_ms);
+        r.last_done_ms = std::max(r.last_done_ms, q.done_ms);
+    }
+    r.submitted = count;
+    r.completed = lat.size();
+    r.admitted = lat.size();
+    r.batches = s->st.batches;
+    r.max_queued = s->st.max_queued;
+    r.budget_in_use = s->arena.used();
+    fill_stats(lat, &r);
+    if (ids)
+        for (uint64_t k = 0; k < count; ++k) ids[k] = mine[k];
+    if (out) *out = r;
+    return TRV_OK;
+}
+
+int32_t trv_server_destroy(trv_server* s) {
+    if (!s) return TRV_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->stop = true;
+        s->wake.notify_one();
+    }
+    if (s->dispatcher.joinable()) s->dispatcher.join();
+    for (Slot& x : s->slots) {
+        if (x.stream) cudaStreamSynchronize(x.stream);
+        free_slot(x);
+    }
+    const int err = s->error;
+    delete s;
+    return err;
+}
+
+}  // extern "C"
