@@ -161,6 +161,7 @@ struct trv_server {
             if (q == cudaErrorNotReady) continue;
             if (q != cudaSuccess && error == TRV_OK) error = cuda_fail(q);
             const double t = now_ms();
+            st.last_done_ms = t;
             for (uint64_t id : s.ids) {
                 Req& r = reqs[id];
                 r.phase = DONE;
