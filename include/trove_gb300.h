@@ -184,6 +184,25 @@ int32_t trv_batch_capture(trv_batch* batch, void* stream);
 int32_t trv_batch_info(const trv_batch* batch, uint64_t* tiles, uint64_t* bytes);
 int32_t trv_batch_destroy(trv_batch* batch);
 
+/* Largest batch trv_batch_run_static accepts. */
+#define TRV_STATIC_BATCH_MAX_TASKS 4096
+
+/* The batch without any device allocation, for callers that cannot call
+ * cudaMalloc: it synchronizes the whole device (stalling latency-critical
+ * loops that share the GPU), and processes whose device memory is reserved
+ * up front by another allocator may have none to spare.  No counterpart in
+ * the reference.  Same tasks, options and results as trv_batch_create +
+ * trv_batch_launch, planned and launched in one call on `stream`; the task
+ * table, tile prefix and work counter live in one library-owned __device__
+ * array (about 300 KB per device, held until the process exits) instead of
+ * cudaMalloc'd memory.  At most TRV_STATIC_BATCH_MAX_TASKS tasks
+ * (TRV_ERR_UNSUPPORTED beyond).  Every call on a device shares that array and
+ * clears its counter on `stream`: calls whose work overlaps on the GPU race
+ * and must be ordered by the caller.  The first call on a device looks up the
+ * array's address (once per device); make it before any stream capture. */
+int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
+                             void* stream);
+
 /* Baseline for the batch: one plain launch per task (trv_copy / trv_gather /
  * trv_scatter, AUTO path), in order, on `stream`. */
 int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream);

@@ -1,0 +1,84 @@
+"""trv_batch_run_static: the batch entry point that allocates no device
+memory, for callers that cannot call cudaMalloc (it synchronizes the whole
+device; a process whose device memory is reserved up front by another
+allocator may have none to spare).  Its results must equal the allocating
+entry point's (trv_batch_create + trv_batch_launch) byte for byte, on two
+calls in a row, since every call reuses the same library-owned device array.
+Collected last so that a run stopping at the first failure has run the rest."""
+import numpy as np
+import pytest
+
+import oracle
+import trove_gb300 as tg
+
+pytestmark = pytest.mark.gpu
+
+SENTINEL = 0x5A
+
+
+def workload(torch, count, seed):
+    rng = np.random.default_rng(seed)
+    tasks = []
+    for k in range(count):
+        op = int(rng.choice([0, 0, 1, 1, 2]))
+        w = int(rng.choice([4, 8, 12, 20, 36, 48, 64]))
+        n = int(np.exp(rng.uniform(0, np.log(30000))))
+        src = torch.from_numpy(oracle.random_structs(n, w, seed=seed * 977 + k).reshape(-1).copy()).cuda()
+        dst = torch.full((n * w,), SENTINEL, dtype=torch.uint8, device="cuda")
+        idx = None
+        if op == 1:
+            idx = torch.from_numpy(oracle.uniform_indices(n, n, seed + k)).cuda()
+        elif op == 2:
+            idx = torch.from_numpy(oracle.permutation(n, seed + k)).cuda()
+        tasks.append(dict(op=op, width=w, n=n, src=src, dst=dst, idx=idx, bound=n))
+    return tasks
+
+
+def outputs(tasks):
+    return [t["dst"].cpu().numpy().copy() for t in tasks]
+
+
+def reset(tasks):
+    for t in tasks:
+        t["dst"].fill_(SENTINEL)
+
+
+def test_static_batch_equals_allocating_batch(cuda):
+    torch = cuda
+    tasks = workload(torch, 300, seed=21)
+    b = tg.Batch(tasks, tile_bytes=16384)
+    b.launch()
+    torch.cuda.synchronize()
+    expect = outputs(tasks)
+    b.close()
+    for call in range(2):
+        reset(tasks)
+        tg.run_static(tasks, tile_bytes=16384)
+        torch.cuda.synchronize()
+        for k, (got, e) in enumerate(zip(outputs(tasks), expect)):
+            assert np.array_equal(got, e), (call, k, tasks[k]["op"], tasks[k]["width"], tasks[k]["n"])
+    # a different batch through the same array right after, with default tiles
+    more = workload(torch, 40, seed=22)
+    b = tg.Batch(more)
+    b.launch()
+    torch.cuda.synchronize()
+    expect = outputs(more)
+    b.close()
+    reset(more)
+    tg.run_static(more)
+    torch.cuda.synchronize()
+    for got, e in zip(outputs(more), expect):
+        assert np.array_equal(got, e)
+
+
+def test_static_batch_limit(cuda):
+    torch = cuda
+    src = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    dst = torch.zeros_like(src)
+    one = dict(op=0, width=4, n=16, src=src, dst=dst)
+    with pytest.raises(tg.TroveError) as e:
+        tg.run_static([one] * (tg.STATIC_BATCH_MAX_TASKS + 1))
+    assert e.value.status == 2  # TRV_ERR_UNSUPPORTED
+    tg.run_static([one] * tg.STATIC_BATCH_MAX_TASKS)
+    torch.cuda.synchronize()
+    assert torch.equal(dst, src)

@@ -112,6 +112,8 @@ _SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "trv_batch_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
     "trv_run_per_call": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_batch_run_static": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.POINTER(BatchOptions),
+                                              ctypes.c_void_p]),
     "trv_autotune_call": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]),
     "trv_autotune_batch": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.c_void_p]),
     "trv_autotune_lookup": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64,
@@ -291,6 +293,22 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+STATIC_BATCH_MAX_TASKS = 4096
+
+
+def run_static(tasks, *, tile_bytes: int = 0, grid: int = 0, blocks_per_sm: int = 0, stream=None):
+    """Plan and run a batch in one call without allocating device memory
+    (trv_batch_run_static), for callers that must not call cudaMalloc: it
+    synchronizes the whole device, and a process whose device memory is
+    reserved up front by another allocator may have none to spare.  Uses one
+    library-owned device array of at most STATIC_BATCH_MAX_TASKS task entries,
+    shared by every call on the device: calls whose work overlaps on the GPU
+    race and must be ordered by the caller."""
+    arr = make_tasks(tasks)
+    opt = BatchOptions(int(tile_bytes), PATH_AUTO, int(grid), int(blocks_per_sm))
+    _check(load().trv_batch_run_static(arr, len(arr), ctypes.byref(opt), _stream(stream)), "trv_batch_run_static")
 
 
 def run_per_call(tasks, stream=None):
