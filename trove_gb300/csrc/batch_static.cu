@@ -98,7 +98,7 @@ int plan_static(const trv_task* tasks, uint64_t count, const trv_batch_options* 
         if (tuned && c.grid == 2) vote2 += tb;
         if (tuned && c.grid == 4) vote4 += tb;
     }
-    *blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote2 > vote4 ? 2 : 4);
+    *blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote4 > vote2 ? 4 : 2);
     return TRV_OK;
 }
 

@@ -239,7 +239,7 @@ struct trv_server {
             if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), s.stream);
             if (e == cudaSuccess) {
                 const int g = tiles < grid ? int(tiles > 0 ? tiles : 1) : grid;
-                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, 4, s.stream);
+                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, 2, s.stream);
             }
             if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
             if (e != cudaSuccess && error == TRV_OK) error = cuda_fail(e);
@@ -348,7 +348,7 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
         }
     }
     // Concurrent batches share the GPU: each gets an equal part of it.
-    const int resident = resident_blocks(batch_kernel_func(4), batch_block_threads());
+    const int resident = resident_blocks(batch_kernel_func(2), batch_block_threads());
     s->grid = std::max(1, resident / s->cfg.max_inflight);
     s->t0 = clock_type::now();
     s->dispatcher = std::thread([s] { s->run(); });
