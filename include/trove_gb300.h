@@ -80,6 +80,15 @@ int32_t trv_version(void);
 /* Last CUDA error code seen by this thread's calls (0 if none). */
 int32_t trv_last_cuda_error(void);
 
+/* Sets the current context's L2 fetch granularity hint (bytes: 32, 64 or 128;
+ * cudaLimitMaxL2FetchGranularity) and returns the previous value in
+ * *previous (may be NULL).  A random gather reads one struct per location, so
+ * a fetch of 32 bytes instead of a whole 128-byte line can halve its DRAM
+ * traffic; streaming copies are unaffected.  It is a per-process context
+ * setting (released with the context), applies to every kernel the context
+ * runs afterwards, and may synchronize the device: set it once at start-up. */
+int32_t trv_set_l2_fetch_granularity(int32_t bytes, int32_t* previous);
+
 /* Synchronizes `stream`, then reads and clears the current device's error
  * flag, which a kernel sets when one of its bounded waits gives up (the TMA
  * bulk path).  TRV_ERR_DEVICE_FLAG if it was set. */
@@ -107,6 +116,9 @@ int32_t trv_copy_exit_ex(void* dst, const void* src, uint64_t n, uint32_t width,
                          const trv_launch* cfg, void* stream);
 
 /* dst[i] = src[idx[i]] for i < n; idx[i] outside [0, src_n) is skipped.
+ * Widths 4..64 in steps of 4 have per-width kernels; wider multiples of 4
+ * use the row-form kernel with a run-time word count; other widths a
+ * byte-wise kernel.
  * Replaces the coalesced_ptr gather kernel (reference trove/ptr.h:76-90,
  * tests/benchmark.cu:90-99). */
 int32_t trv_gather(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n,
@@ -121,6 +133,16 @@ int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* i
                     uint32_t width, void* stream);
 int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n,
                        uint32_t width, const trv_launch* cfg, void* stream);
+
+/* Layout conversion for structs of width/4 32-bit fields (width a multiple
+ * of 4, at most 64): field j of struct i is aos[i].field[j] and
+ * soa[j * n + i].  The AoS side moves through the device API
+ * (load/store_warp_contiguous), the SoA side as one coalesced stream per
+ * field.  The reference's block interface exists for such per-thread array
+ * producers and consumers (README "Block Interface"); these entry points are
+ * the conversion kernels users of it write by hand. */
+int32_t trv_aos_to_soa(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, void* stream);
+int32_t trv_soa_to_aos(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, void* stream);
 
 /* Synthetic inputs: dst[k] = word k of the seeded splitmix64 stream (the same
  * stream the CPU oracle generates).  No reference counterpart. */

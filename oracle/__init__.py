@@ -49,6 +49,7 @@ def lib():
         c.orc_counting.argtypes = [_u8p, ctypes.c_uint64, ctypes.c_int]
         c.orc_load_sum.argtypes = [_u8p, _u8p, ctypes.c_uint64, ctypes.c_int]
         c.orc_r2c_source.argtypes = [ctypes.c_int, ctypes.c_int, _u8p, _u8p]
+        c.orc_aos_to_soa.argtypes = [_u8p, _u8p, ctypes.c_uint64, ctypes.c_int]
         c.orc_run_mt.argtypes = [ctypes.c_int, _u8p, _u8p, _u8p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int]
         _c = c
     return _c
@@ -133,6 +134,12 @@ def counting(n: int, s: int) -> np.ndarray:
 def load_sum(src: np.ndarray, n: int, s: int) -> np.ndarray:
     out = np.empty(n, np.int32)
     lib().orc_load_sum(_p(np.ascontiguousarray(src).view(np.int32)), _p(out), n, s)
+    return out
+
+
+def aos_to_soa(aos: np.ndarray, n: int, s: int) -> np.ndarray:
+    out = np.empty(n * s, np.uint32)
+    lib().orc_aos_to_soa(_p(out), _p(np.ascontiguousarray(aos).view(np.uint32)), n, s)
     return out
 
 

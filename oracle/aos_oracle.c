@@ -171,6 +171,14 @@ void orc_r2c_source(int n, int m, int32_t* src_lane, int32_t* src_elem) {
         }
 }
 
+/* AoS -> SoA for structs of s 32-bit fields: soa[j*n + i] = aos[i*s + j]
+ * (the conversion a block-interface producer/consumer kernel performs; the
+ * reference's README "Block Interface"). */
+void orc_aos_to_soa(uint32_t* soa, const uint32_t* aos, uint64_t n, int s) {
+    for (uint64_t i = 0; i < n; ++i)
+        for (int j = 0; j < s; ++j) soa[(uint64_t)j * n + i] = aos[i * (uint64_t)s + j];
+}
+
 /* ---- multithreaded forms, for the timed CPU baseline --------------------- */
 
 typedef struct {

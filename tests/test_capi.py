@@ -67,6 +67,10 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.copy(ok, ok, 5, 12, block=128)) == 2
     assert rc_of(lambda: tg.fill_random_u32(0, 5, 1)) == 1
     assert rc_of(lambda: tg.copy_host(0, ok, 5, 4)) == 1
+    assert rc_of(lambda: tg.aos_to_soa(ok, ok, 5, 68)) == 2
+    assert rc_of(lambda: tg.soa_to_aos(ok, bad, 5, 12)) == 3
+    assert rc_of(lambda: tg.aos_to_soa(0, ok, 5, 12)) == 1
+    assert rc_of(lambda: tg.set_l2_fetch_granularity(48)) == 1
 
 
 def test_error_carries_status_text(trove_lib):

@@ -248,3 +248,48 @@ def test_config1_contiguous_copy_12B(cuda):
     tg.copy(dst, src, n, width, path="warp")
     torch.cuda.synchronize()
     assert np.array_equal(to_host(dst), oracle.copy(src_h, n, width))
+
+
+@pytest.mark.parametrize("width", WIDTHS)
+def test_aos_soa_round_trip(cuda, width):
+    torch = cuda
+    s = width // 4
+    for n in [1, 33, 4097, 100003]:
+        aos_h = oracle.random_structs(n, width, seed=width + 7 * n)
+        soa_expect = oracle.aos_to_soa(aos_h, n, s)
+        assert np.array_equal(soa_expect.reshape(s, n), aos_h.view(np.uint32).reshape(n, s).T)
+        aos = to_dev(torch, aos_h)
+        soa = torch.empty(n * width, dtype=torch.uint8, device="cuda")
+        tg.aos_to_soa(soa, aos, n, width)
+        assert np.array_equal(to_host(soa).view(np.uint32), soa_expect), (width, n)
+        back = torch.zeros_like(aos)
+        tg.soa_to_aos(back, soa, n, width)
+        assert np.array_equal(to_host(back), aos_h.reshape(-1)), (width, n)
+
+
+@pytest.mark.parametrize("width", [68, 96, 128, 132, 200, 256])
+def test_index_ops_wide_structs(cuda, width):
+    """Widths above 64 bytes: row-form kernels with a run-time word count."""
+    torch = cuda
+    n = 3000
+    src_h = oracle.random_structs(n, width, seed=width)
+    src = to_dev(torch, src_h)
+    init = np.full(n * width, SENTINEL, np.uint8)
+    for name, idx_h in index_sets(n, seed=width).items():
+        idx = torch.from_numpy(idx_h).cuda()
+        for path in ["auto", "warp"]:
+            dst = to_dev(torch, init)
+            tg.gather(dst, src, n, idx, n, width, path=path)
+            assert np.array_equal(to_host(dst), oracle.gather(init, src_h, idx_h, n, width)), (name, path)
+        if name in ("perm", "identity"):
+            dst = to_dev(torch, init)
+            tg.scatter(dst, n, src, idx, n, width)
+            assert np.array_equal(to_host(dst), oracle.scatter(init, src_h, idx_h, n, width)), name
+    bad = oracle.uniform_indices(n, n, 1).copy()
+    bad[::7] = -3
+    dst = to_dev(torch, init)
+    tg.gather(dst, src, n, torch.from_numpy(bad).cuda(), n, width)
+    e = init.reshape(n, width).copy()
+    ok = bad >= 0
+    e[ok] = src_h[bad[ok]]
+    assert np.array_equal(to_host(dst), e.reshape(-1))

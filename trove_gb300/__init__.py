@@ -81,6 +81,7 @@ _SIGNATURES = {
     "trv_version": (ctypes.c_int32, []),
     "trv_last_cuda_error": (ctypes.c_int32, []),
     "trv_check_device": (ctypes.c_int32, [ctypes.c_void_p]),
+    "trv_set_l2_fetch_granularity": (ctypes.c_int32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "trv_copy": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                   ctypes.c_void_p]),
     "trv_copy_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
@@ -101,6 +102,10 @@ _SIGNATURES = {
                                         ctypes.c_void_p]),
     "trv_fill_random_u32": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                              ctypes.c_void_p]),
+    "trv_aos_to_soa": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_void_p]),
+    "trv_soa_to_aos": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_void_p]),
     "trv_fill_uniform_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                                   ctypes.c_void_p]),
     "trv_copy_host": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32]),
@@ -199,6 +204,14 @@ def copy(dst, src, n: int, width: int, *, path=PATH_AUTO, unroll: int = 0, block
                            _stream(stream)), "trv_copy")
 
 
+def set_l2_fetch_granularity(nbytes: int) -> int:
+    """Set the context's L2 fetch granularity hint (32, 64 or 128 bytes);
+    returns the previous value."""
+    prev = ctypes.c_int32()
+    _check(load().trv_set_l2_fetch_granularity(int(nbytes), ctypes.byref(prev)), "trv_set_l2_fetch_granularity")
+    return prev.value
+
+
 def check_device(stream=None):
     """Synchronize and raise if a kernel's bounded wait gave up."""
     _check(load().trv_check_device(_stream(stream)), "trv_check_device")
@@ -231,6 +244,16 @@ def scatter(dst, dst_n: int, src, idx, n: int, width: int, *, path=PATH_AUTO, un
 def fill_random_u32(dst, nwords: int, seed: int, *, stream=None):
     """dst[k] = word k of the seeded splitmix64 stream."""
     _check(load().trv_fill_random_u32(_addr(dst), nwords, seed, _stream(stream)), "trv_fill_random_u32")
+
+
+def aos_to_soa(dst_soa, src_aos, n: int, width: int, *, stream=None):
+    """soa[j * n + i] = field j of struct i (32-bit fields)."""
+    _check(load().trv_aos_to_soa(_addr(dst_soa), _addr(src_aos), n, width, _stream(stream)), "trv_aos_to_soa")
+
+
+def soa_to_aos(dst_aos, src_soa, n: int, width: int, *, stream=None):
+    """Field j of struct i = soa[j * n + i] (32-bit fields)."""
+    _check(load().trv_soa_to_aos(_addr(dst_aos), _addr(src_soa), n, width, _stream(stream)), "trv_soa_to_aos")
 
 
 def fill_uniform_indices(idx, n: int, bound: int, seed: int, *, stream=None):

@@ -195,6 +195,17 @@ int32_t trv_version(void) { return 100; }
 
 int32_t trv_last_cuda_error(void) { return g_last_cuda_error; }
 
+int32_t trv_set_l2_fetch_granularity(int32_t bytes, int32_t* previous) {
+    if (bytes != 32 && bytes != 64 && bytes != 128) return TRV_ERR_INVALID_ARGUMENT;
+    size_t old = 0;
+    cudaError_t e = cudaDeviceGetLimit(&old, cudaLimitMaxL2FetchGranularity);
+    if (e != cudaSuccess) return cuda_fail(e);
+    e = cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, size_t(bytes));
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (previous) *previous = int32_t(old);
+    return TRV_OK;
+}
+
 int32_t trv_check_device(void* stream) {
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e);
@@ -293,6 +304,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
     if (c.block_threads != 0 && c.block_threads != 256) return TRV_ERR_UNSUPPORTED;
     if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
     const bool structs = struct_width(width) && aligned(dst, 4) && aligned(src, 4);
+    const bool wide_words = width % 4 == 0 && width > 64 && aligned(dst, 4) && aligned(src, 4);
     if (c.path == TRV_PATH_AUTO) {
         TuneChoice t;
         if (structs && tune_lookup(TuneKey{SCOPE_CALL, gather ? TRV_OP_GATHER : TRV_OP_SCATTER, int(width),
@@ -300,7 +312,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
                                    &t))
             c = trv_launch{t.path, t.unroll, 0, t.grid, 0, t.cache_policy};
         else
-            c.path = structs ? TRV_PATH_WARP : TRV_PATH_VECTOR;
+            c.path = (structs || wide_words) ? TRV_PATH_WARP : TRV_PATH_VECTOR;
     }
     if (c.cache_policy < 0 || c.cache_policy > 3) return TRV_ERR_INVALID_ARGUMENT;
     const int path = c.path;
@@ -316,6 +328,17 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
         return check_launch();
     }
     if (path != TRV_PATH_COALESCED && path != TRV_PATH_DIRECT && path != TRV_PATH_WARP) return TRV_ERR_UNSUPPORTED;
+    if (path == TRV_PATH_WARP && width % 4 == 0 && width > 64) {  // run-time word count
+        if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
+        int wb = 16;
+        while (wb > 4 && (width % uint32_t(wb) != 0 || !aligned(dst, uintptr_t(wb)) || !aligned(src, uintptr_t(wb))))
+            wb >>= 1;
+        const long long warps = (long long)((n + 31) / 32);
+        const int grid = grid_for(index_rows_rt_func(gather, wb), warps, 8, 256, grid_req);
+        launch_index_rows_rt(gather, wb, IndexArgs{src, dst, idx, (long long)n, (long long)bound, c.cache_policy},
+                             int(width / uint32_t(wb)), grid, st);
+        return check_launch();
+    }
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
     const int u = c.unroll > 0 ? c.unroll : default_unroll(width);
@@ -355,6 +378,28 @@ int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t
 int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* idx, uint64_t n, uint32_t width,
                     void* stream) {
     return index_op(false, dst, src, dst_n, idx, n, width, nullptr, stream);
+}
+
+static int32_t layout_op(bool to_soa, void* dst, const void* src, uint64_t n, uint32_t width, void* stream) {
+    if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
+    if (n == 0) return TRV_OK;
+    if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
+    if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
+    if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
+    const int u = default_unroll(width);
+    const WidthOps* ops = ops_for_words(int(width / 4));
+    const CopyKernel& k = to_soa ? ops->aos_to_soa[unroll_slot(u)] : ops->soa_to_aos[unroll_slot(u)];
+    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, 0);
+    k.launch(CopyArgs{src, dst, (long long)n, 0u}, grid, 256, static_cast<cudaStream_t>(stream));
+    return check_launch();
+}
+
+int32_t trv_aos_to_soa(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, void* stream) {
+    return layout_op(true, dst_soa, src_aos, n, width, stream);
+}
+
+int32_t trv_soa_to_aos(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, void* stream) {
+    return layout_op(false, dst_aos, src_soa, n, width, stream);
 }
 
 int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint64_t seed, void* stream) {

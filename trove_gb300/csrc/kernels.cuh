@@ -377,4 +377,107 @@ scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* _
     }
 }
 
+// Row-form gather / scatter with the word count m given at run time: one
+// kernel per word type serves every width that is a multiple of 4 bytes,
+// including structs wider than the per-width tables cover (> 64 bytes).  Same
+// scheme as the compile-time kernels above; the m rounds of a chunk run in
+// groups of G so the live registers stay bounded for any m.
+template <typename V, int G, bool GATHER>
+__global__ void __launch_bounds__(256)
+index_rows_rt_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* __restrict__ dst, long long bound,
+                     long long n, int m, int policy) {
+    const WarpGrid g;
+    const unsigned long long pol = policy == 3 ? l2_evict_last_policy() : 0ull;
+    for (long long base = g.warp * 32; base < n; base += g.warps * 32) {
+        const long long i = base + g.lane;
+        const int v = i < n ? ld_index(idx + i, policy) : -1;
+        const int id = (v >= 0 && (long long)v < bound) ? v : -1;
+        for (int k0 = 0; k0 < m; k0 += G) {
+            V val[G];
+            int other[G];
+#pragma unroll
+            for (int t = 0; t < G; ++t) {
+                const int k = k0 + t;
+                other[t] = -1;
+                if (k < m) {  // m is uniform: the whole warp takes the same branch
+                    const int q = g.lane + 32 * k;
+                    const int j = q / m;
+                    other[t] = __shfl_sync(0xFFFFFFFFu, id, j);
+                    if (other[t] >= 0)
+                        val[t] = GATHER ? ld_random(src + (long long)other[t] * m + (q - j * m), policy, pol)
+                                        : ld_contig(src + base * m + q, policy);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < G; ++t) {
+                if (other[t] < 0) continue;
+                const int q = g.lane + 32 * (k0 + t);
+                if (GATHER)
+                    st_contig(dst + base * m + q, val[t], policy);
+                else
+                    st_random(dst + (long long)other[t] * m + (q % m), val[t], policy, pol);
+            }
+        }
+    }
+}
+
+// AoS <-> SoA for structs of S 32-bit fields: field j of struct i sits at
+// aos[i].word(j) and soa[j * n + i].  The AoS side moves through the device
+// API (load/store_warp_contiguous: coalesced rounds + transpose); the SoA side
+// is S coalesced 32-bit streams, one per field.
+template <int S, int U>
+__global__ void __launch_bounds__(256)
+aos_to_soa_kernel(const aos<S>* __restrict__ src, unsigned* __restrict__ dst, long long n) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        aos<S> v[U];
+        const bool full = base + CH <= n;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            if (full)
+                v[u] = trove::load_warp_contiguous(src + i);
+            else if (i < n)
+                v[u] = trove::detail::divergent_load(src + i);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            if (!full && i >= n) continue;
+            const trove::detail::regs<unsigned, S> w = trove::detail::to_regs(v[u]);
+#pragma unroll
+            for (int j = 0; j < S; ++j) __stcs(dst + (long long)j * n + i, w.v[j]);
+        }
+    }
+}
+
+template <int S, int U>
+__global__ void __launch_bounds__(256)
+soa_to_aos_kernel(const unsigned* __restrict__ src, aos<S>* __restrict__ dst, long long n) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
+        const bool full = base + CH <= n;
+        trove::detail::regs<unsigned, S> w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            if (full || i < n) {
+#pragma unroll
+                for (int j = 0; j < S; ++j) w[u].v[j] = __ldcs(src + (long long)j * n + i);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + g.lane;
+            const aos<S> v = trove::detail::from_regs(w[u]);
+            if (full)
+                trove::store_warp_contiguous(v, dst + i);
+            else if (i < n)
+                trove::detail::divergent_store(v, dst + i);
+        }
+    }
+}
+
 }  // namespace trv

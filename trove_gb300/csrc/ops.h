@@ -44,7 +44,14 @@ struct WidthOps {
     IndexKernel gather_rows[2][kUnrolls];
     IndexKernel scatter_rows[2][kUnrolls];
     int rows_word_bytes;  // size of the word used by slot [0]
+    CopyKernel aos_to_soa[kUnrolls];
+    CopyKernel soa_to_aos[kUnrolls];
 };
+
+// Row-form gather / scatter with a run-time word count (rows_rt.cu), for any
+// width that is a multiple of 4 bytes.  word_bytes: 16, 8 or 4.
+void launch_index_rows_rt(bool gather, int word_bytes, const IndexArgs& a, int m, int grid, cudaStream_t st);
+const void* index_rows_rt_func(bool gather, int word_bytes);
 
 // Defined in width_ops.cu, one specialisation per translation unit.
 template <int S>

@@ -89,6 +89,25 @@ void fill_rows(IndexKernel (&g)[kUnrolls], IndexKernel (&s)[kUnrolls]) {
     rows_entries<V, 3>(g[3], s[3]);
 }
 
+template <int U>
+void launch_aos_to_soa(const CopyArgs& a, int grid, int block, cudaStream_t st) {
+    aos_to_soa_kernel<S, U><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src), static_cast<unsigned*>(a.dst),
+                                                    a.n);
+}
+
+template <int U>
+void launch_soa_to_aos(const CopyArgs& a, int grid, int block, cudaStream_t st) {
+    soa_to_aos_kernel<S, U><<<grid, block, 0, st>>>(static_cast<const unsigned*>(a.src), static_cast<aos<S>*>(a.dst),
+                                                    a.n);
+}
+
+template <int k>
+void layout_entries(CopyKernel& to_soa, CopyKernel& to_aos) {
+    constexpr int U = unroll_for(k);
+    to_soa = {&launch_aos_to_soa<U>, (const void*)&aos_to_soa_kernel<S, U>};
+    to_aos = {&launch_soa_to_aos<U>, (const void*)&soa_to_aos_kernel<S, U>};
+}
+
 template <int API, bool EXIT>
 void fill_copy(CopyKernel (&row)[kUnrolls]) {
     row[0] = copy_entry<API, EXIT, 0>();
@@ -133,6 +152,10 @@ WidthOps make_ops() {
     fill_rows<typename word_of<kWideWord>::type>(ops.gather_rows[0], ops.scatter_rows[0]);
     fill_rows<unsigned>(ops.gather_rows[1], ops.scatter_rows[1]);
     ops.rows_word_bytes = kWideWord;
+    layout_entries<0>(ops.aos_to_soa[0], ops.soa_to_aos[0]);
+    layout_entries<1>(ops.aos_to_soa[1], ops.soa_to_aos[1]);
+    layout_entries<2>(ops.aos_to_soa[2], ops.soa_to_aos[2]);
+    layout_entries<3>(ops.aos_to_soa[3], ops.soa_to_aos[3]);
     return ops;
 }
 
