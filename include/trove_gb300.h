@@ -94,6 +94,14 @@ int32_t trv_set_l2_fetch_granularity(int32_t bytes, int32_t* previous);
  * bulk path).  TRV_ERR_DEVICE_FLAG if it was set. */
 int32_t trv_check_device(void* stream);
 
+/* Testing hook for the bounded waits of the TMA bulk path: the copy loop's
+ * mbarrier waits give up after `polls` polls (0xFFFFFFFF restores the default
+ * of about a second).  A wait that gives up sets the device flag that
+ * trv_check_device reports; the kernel still waits (with the default budget)
+ * for every transfer it has in flight before it exits, so the context stays
+ * usable.  With 0 polls every launch reports the flag. */
+int32_t trv_debug_set_bulk_wait_polls(uint32_t polls);
+
 /* dst[i] = src[i] for i < n structs of `width` bytes.
  * Replaces the user kernel `T v = load_warp_contiguous(src + i);
  * store_warp_contiguous(v, dst + i);` (reference trove/aos.h:66-105,

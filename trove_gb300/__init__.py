@@ -81,6 +81,7 @@ _SIGNATURES = {
     "trv_version": (ctypes.c_int32, []),
     "trv_last_cuda_error": (ctypes.c_int32, []),
     "trv_check_device": (ctypes.c_int32, [ctypes.c_void_p]),
+    "trv_debug_set_bulk_wait_polls": (ctypes.c_int32, [ctypes.c_uint32]),
     "trv_set_l2_fetch_granularity": (ctypes.c_int32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "trv_copy": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                   ctypes.c_void_p]),
@@ -210,6 +211,11 @@ def set_l2_fetch_granularity(nbytes: int) -> int:
     prev = ctypes.c_int32()
     _check(load().trv_set_l2_fetch_granularity(int(nbytes), ctypes.byref(prev)), "trv_set_l2_fetch_granularity")
     return prev.value
+
+
+def debug_set_bulk_wait_polls(polls: int):
+    """Testing hook: poll budget of the bulk copy's waits (0xFFFFFFFF: default)."""
+    _check(load().trv_debug_set_bulk_wait_polls(polls & 0xFFFFFFFF), "trv_debug_set_bulk_wait_polls")
 
 
 def check_device(stream=None):

@@ -42,10 +42,10 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
                  : "memory");
 }
 
-// true once the phase with the given parity has completed; false after the
-// poll budget is spent.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    for (unsigned i = 0; i < kSpinLimit; ++i) {
+// true once the phase with the given parity has completed; false after
+// `polls` unsuccessful polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned polls = kSpinLimit) {
+    for (unsigned i = 0; i < polls; ++i) {
         unsigned done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -79,7 +79,7 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 
 __global__ void __launch_bounds__(32)
 bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, long long nbytes, int head,
-                 int chunk, int* flag) {
+                 int chunk, int* flag, unsigned polls) {
     extern __shared__ __align__(128) unsigned char stage_mem[];
     __shared__ __align__(8) unsigned long long bar[kStages];
 
@@ -120,7 +120,7 @@ bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restric
     long long k = 0;
     for (; k < mine; ++k) {
         const int st = int(k % kStages);
-        if (!mbar_wait(&bar[st], unsigned((k / kStages) & 1))) {
+        if (!mbar_wait(&bar[st], unsigned((k / kStages) & 1), polls)) {
             ok = false;
             break;
         }
@@ -134,9 +134,10 @@ bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restric
     }
     if (!ok) {
         atomicExch(flag, 1);
-        // drain loads still in flight (bounded), so no transfer targets this
-        // CTA's shared memory after it exits
-        for (long long j = k + 1; j < issued; ++j) mbar_wait(&bar[j % kStages], unsigned((j / kStages) & 1));
+        // drain every load still in flight, including the one that timed out
+        // (bounded), so no transfer targets this CTA's shared memory after it
+        // exits
+        for (long long j = k; j < issued; ++j) mbar_wait(&bar[j % kStages], unsigned((j / kStages) & 1));
     }
     bulk_wait_all();
 }
@@ -149,6 +150,12 @@ bool bulk_copy_supported(const void* src, const void* dst) {
 
 int bulk_copy_smem_bytes(int chunk) { return kStages * chunk; }
 
+namespace {
+unsigned g_main_polls = kSpinLimit;
+}
+
+void set_bulk_wait_polls(unsigned polls) { g_main_polls = polls == 0xFFFFFFFFu ? kSpinLimit : polls; }
+
 cudaError_t launch_bulk_copy(const void* src, void* dst, long long nbytes, int chunk, int grid, int* flag,
                              cudaStream_t st) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(src);
@@ -158,7 +165,7 @@ cudaError_t launch_bulk_copy(const void* src, void* dst, long long nbytes, int c
     cudaError_t e = cudaFuncSetAttribute(bulk_copy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     bulk_copy_kernel<<<grid, 32, smem, st>>>(static_cast<const unsigned char*>(src), static_cast<unsigned char*>(dst),
-                                             nbytes, head, chunk, flag);
+                                             nbytes, head, chunk, flag, g_main_polls);
     return cudaGetLastError();
 }
 

@@ -206,6 +206,11 @@ int32_t trv_set_l2_fetch_granularity(int32_t bytes, int32_t* previous) {
     return TRV_OK;
 }
 
+int32_t trv_debug_set_bulk_wait_polls(uint32_t polls) {
+    set_bulk_wait_polls(polls);
+    return TRV_OK;
+}
+
 int32_t trv_check_device(void* stream) {
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e);
