@@ -302,7 +302,7 @@ class Sweep:
         h_src = torch.empty(ab, dtype=torch.uint8).pin_memory()
         h_dst = torch.empty(ab, dtype=torch.uint8).pin_memory()
         h_src.copy_(self.src[:ab].cpu())
-        tg.copy_host(h_dst, h_src, ab // 64, 64)  # warm the staging ring
+        tg.copy_host(h_dst, h_src, ab // 64, 64)  # warm-up: pins the path and pages the buffers in
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -314,7 +314,7 @@ class Sweep:
         io = sum(n * w for s, w, n in self.plan)
         return {"value": round(steps * 2 * io * world / el / 1e9, 2), "unit": UNIT, "h2d_bytes_per_step": io,
                 "d2h_bytes_per_step": io, "steps": steps,
-                "path": "trv_copy_host per width: pinned host buffers, chunked H2D / copy kernel / D2H overlap"}
+                "path": "trv_copy_host per width: pinned host buffers, read and written in place by the copy kernel over the CPU-GPU link"}
 
     def extra(self):
         return {"tuned_unroll": self.tuned}
@@ -331,15 +331,16 @@ class Gather:
     }
 
     def __init__(self, torch, tg, dev, args):
-        import oracle  # index patterns for the workload come from the seeded generators
         self.torch, self.tg, self.dev = torch, tg, dev
         n = GATHER_N
         self.src = torch.empty(n * 64 + 256, dtype=torch.uint8, device=dev)
         tg.fill_random_u32(self.src, (n * 64 + 256) // 4, seed=0)
         self.dst = torch.empty(n * 64, dtype=torch.uint8, device=dev)
-        self.idx = {"perm": torch.from_numpy(oracle.permutation(n, 1)).to(dev),
-                    "runs": torch.from_numpy(oracle.run_indices(n, 2)).to(dev),
-                    "identity": torch.arange(n, dtype=torch.int32, device=dev)}
+        self.idx = {p: torch.empty(n, dtype=torch.int32, device=dev) for p in GATHER_PATTERNS}
+        tg.fill_permutation(self.idx["perm"], n, 1)
+        tg.fill_run_indices(self.idx["runs"], n, 2)
+        self.idx["identity"].copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        torch.cuda.synchronize(dev)
         self.tuned = {}
 
     def tune(self):
@@ -439,6 +440,7 @@ class Batch:
             elif op == 2:
                 idx = torch.randperm(n, generator=gen, device=dev, dtype=torch.int32)
             self.tasks.append(dict(op=op, width=w, n=n, src=src, dst=dst, idx=idx, bound=n))
+        torch.cuda.synchronize(dev)  # inputs ready before any side stream reads them
         self.stream = torch.cuda.Stream(dev)
         self.batch = None
         self.per_call_ms = None
@@ -459,6 +461,9 @@ class Batch:
             self.build()
         for t in self.tasks:
             t["dst"].fill_(SENTINEL)
+        # the fills ran on the current stream; the batch stream does not wait
+        # for it by itself (torch's side streams are non-blocking)
+        self.stream.wait_stream(torch.cuda.current_stream(self.dev))
         self.batch.launch(self.stream)
         self.stream.synchronize()
         for k, t in enumerate(self.tasks):
@@ -594,6 +599,7 @@ class Serve:
             self.src[w] = t
         self.idx = torch.empty(SERVE_POOL, dtype=torch.int32, device=dev)
         tg.fill_uniform_indices(self.idx, SERVE_POOL, SERVE_POOL, seed=3)
+        torch.cuda.synchronize(dev)  # the server's streams do not order after this one
         self.ptrs = {w: t.data_ptr() for w, t in self.src.items()}
         self.rows = []
 

@@ -159,11 +159,20 @@ int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void*
 /* Synthetic indices: idx[i] = uniform in [0, bound) from the seeded stream
  * (the oracle's orc_uniform_indices gives the same values).  bound < 2^31. */
 int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint64_t seed, void* stream);
+/* Run pattern (32 <= n < 2^31): each aligned chunk of 32 outputs is, with
+ * probability 1/2, a run start + 0..31 (start uniform in [0, n - 32]), else
+ * 32 independent indices uniform in [0, n).  Device kernel, stream-ordered. */
+int32_t trv_fill_run_indices(int32_t* idx, uint64_t n, uint64_t seed, void* stream);
+/* Seeded Fisher-Yates permutation of 0..n-1 (n < 2^31), computed on the host
+ * and copied to idx on `stream`; returns after the copy. */
+int32_t trv_fill_permutation(int32_t* idx, uint64_t n, uint64_t seed, void* stream);
 
-/* Host-buffer copy: src_host -> device staging -> copy kernel -> dst_host,
- * chunked and overlapped on internal streams; returns when dst_host holds
- * the result.  Buffers should be pinned for full speed.  No reference
- * counterpart (the reference has no host API). */
+/* Host-buffer copy; returns when dst_host holds the result.  When the GPU can
+ * address both buffers (pinned memory, or any memory where the GPU uses the
+ * host page tables) the copy kernel reads and writes them in place; otherwise
+ * src_host -> device staging -> copy kernel -> dst_host, chunked and
+ * overlapped on internal streams.  No reference counterpart (the reference
+ * has no host API). */
 int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t n, uint32_t width);
 
 /* ---- batched execution ---------------------------------------------------
@@ -287,7 +296,9 @@ typedef struct trv_server trv_server;
 
 int32_t trv_server_create(const trv_server_config* cfg, trv_server** out);
 /* Queues a request; returns at once.  TRV_ERR_BUDGET if its output alone
- * exceeds the budget. */
+ * exceeds the budget.  The server's streams are not ordered after any caller
+ * stream: the request's source and index arrays must already be complete on
+ * the device (synchronize the stream that wrote them before submitting). */
 int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id);
 /* TRV_OK with the result once done, TRV_ERR_BUSY before, TRV_ERR_NOT_FOUND
  * for an unknown or released id. */

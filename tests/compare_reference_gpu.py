@@ -1,0 +1,169 @@
+"""Side-by-side timing of the reference Trove and this library on one GPU.
+
+Not collected by pytest (no test_ prefix): run it directly on a GB300, after
+the library and the harness cubins are built:
+
+    python tests/compare_reference_gpu.py [--out FILE] [--reps N]
+
+The reference's kernels come from oracle/_ref/trove_ref_kernels.cubin, which
+compiles oracle/trove_bench_kernels.cu (the reference's own test-kernel
+patterns) against the reference's headers; it is built where the reference
+checkout exists and travels with the repository.  This library is called
+through its C ABI, as a user would.  Both sides run the same workloads on the
+same buffers:
+
+* the width sweep: s = 1..16 words, 2 GiB arrays of seeded random words, a
+  lane leaving between load and store when its first word w has
+  w % 625 == 624 (reference kernel `exit_copy_<s>`: load_warp_contiguous /
+  store_warp_contiguous with the warp_converged() fallback; this library:
+  trv_copy_exit on the warp-contiguous path), plus the compiler-generated
+  AoS copy (`direct_copy_<s>`: r[i] = s[i]);
+* the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
+  the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
+  library: trv_gather).
+
+Every pair of outputs is compared bit for bit before anything is timed.
+Timing: CUDA events around each launch on the launching stream, an L2 flush
+(a 512 MiB write) between launches, median of `reps`.  GB/s counts bytes
+read + written (+ 4 per index), the formula of the reference's
+tests/benchmark.cu:283.
+"""
+import argparse
+import ctypes
+import json
+import statistics
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+MODULUS = 625
+SWEEP_BYTES = 1 << 31
+GATHER_N = 1 << 24
+GATHER_WIDTHS = [8, 12, 16, 24, 32, 48, 64]
+SENTINEL = 0xA5
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--part", choices=["all", "sweep", "gather"], default="all")
+    args = ap.parse_args()
+
+    import torch
+
+    import oracle
+    import trove_gb300 as tg
+
+    tg.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.init()
+    ref = oracle.reference_cubin()
+    if ref is None:
+        raise SystemExit("reference cubin not present (build it where the reference checkout exists)")
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        times = []
+        for _ in range(args.reps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(a.elapsed_time(b))
+        return statistics.median(times)
+
+    def cubin(name, grid, *ptrs_and_scalars):
+        ref.launch(name, grid, 256, list(ptrs_and_scalars), stream.cuda_stream)
+
+    rows = []
+    src = torch.empty(SWEEP_BYTES + 256, dtype=torch.uint8, device=dev)
+    tg.fill_random_u32(src, (SWEEP_BYTES + 256) // 4, seed=0)
+    d_ref = torch.empty(SWEEP_BYTES, dtype=torch.uint8, device=dev)
+    d_own = torch.empty_like(d_ref)
+    torch.cuda.synchronize(dev)
+
+    if args.part in ("all", "sweep"):
+        for s in range(1, 17):
+            w = 4 * s
+            n = SWEEP_BYTES // w
+            grid = (n + 255) // 256
+            assert grid * 256 >= n and n * w <= SWEEP_BYTES
+            ps, pr, po = (ctypes.c_void_p(t.data_ptr()) for t in (src, d_ref, d_own))
+
+            def ref_exit():
+                cubin(f"exit_copy_{s}", grid, ps, pr, ctypes.c_longlong(n), ctypes.c_uint(MODULUS))
+
+            def own_exit():
+                tg.copy_exit(d_own, src, n, w, MODULUS, path="warp", stream=stream)
+
+            def ref_direct():
+                cubin(f"direct_copy_{s}", n // 256, ps, pr)  # one struct per thread, whole blocks only
+
+            d_ref.fill_(SENTINEL)
+            d_own.fill_(SENTINEL)
+            ref_exit()
+            own_exit()
+            torch.cuda.synchronize(dev)
+            if not torch.equal(d_ref, d_own):
+                raise SystemExit(f"outputs differ: width sweep {w} B")
+            skipped = None
+            words0 = src[: n * w].view(torch.int32).view(n, s)[:, 0].to(torch.int64) & 0xFFFFFFFF
+            skipped = int(((words0 % MODULUS) == (MODULUS - 1)).sum())
+            alg = n * w + (n - skipped) * w
+            t_ref, t_own = timed(ref_exit), timed(own_exit)
+            t_dir = timed(ref_direct)
+            row = {"workload": "sweep", "width": w, "structs": n,
+                   "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
+                   "ratio": round(t_ref / t_own, 3),
+                   "compiler_aos_copy_gbs": round(2 * (n // 256 * 256) * w / t_dir / 1e6, 1)}
+            rows.append(row)
+            print(json.dumps(row), flush=True)
+
+    if args.part in ("all", "gather"):
+        n = GATHER_N
+        idx = {p: torch.empty(n, dtype=torch.int32, device=dev) for p in ("perm", "runs", "identity")}
+        tg.fill_permutation(idx["perm"], n, 1)
+        tg.fill_run_indices(idx["runs"], n, 2)
+        idx["identity"].copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        torch.cuda.synchronize(dev)
+        for w in GATHER_WIDTHS:
+            s = w // 4
+            assert n * w <= SWEEP_BYTES
+            for p, ix in idx.items():
+                pi, ps, pr = (ctypes.c_void_p(t.data_ptr()) for t in (ix, src, d_ref))
+
+                def ref_gather():
+                    cubin(f"shfl_gather_{s}", n // 256, pi, ps, pr)
+
+                def own_gather():
+                    tg.gather(d_own, src, n, ix, n, w, stream=stream)
+
+                ref_gather()
+                own_gather()
+                torch.cuda.synchronize(dev)
+                if not torch.equal(d_ref[: n * w], d_own[: n * w]):
+                    raise SystemExit(f"outputs differ: gather {w} B {p}")
+                alg = (2 * w + 4) * n
+                t_ref, t_own = timed(ref_gather), timed(own_gather)
+                row = {"workload": "gather", "width": w, "pattern": p,
+                       "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
+                       "ratio": round(t_ref / t_own, 3)}
+                rows.append(row)
+                print(json.dumps(row), flush=True)
+
+    tg.check_device()
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "rows": rows}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -223,6 +223,22 @@ def test_uniform_indices_match_oracle(cuda):
         assert np.array_equal(to_host(t), oracle.uniform_indices(n, bound, seed))
 
 
+def test_run_indices_and_permutation_match_oracle(cuda):
+    """The gather workload's index patterns, generated by the library, equal
+    the oracle's generators (ragged last chunk included)."""
+    torch = cuda
+    for n, seed in [(32, 0), (33, 4), (100003, 2), (1 << 20, 7)]:
+        t = torch.empty(n, dtype=torch.int32, device="cuda")
+        tg.fill_run_indices(t, n, seed)
+        assert np.array_equal(to_host(t), oracle.run_indices(n, seed))
+    for n, seed in [(1, 0), (2, 5), (100003, 1), (1 << 20, 3)]:
+        t = torch.empty(n, dtype=torch.int32, device="cuda")
+        tg.fill_permutation(t, n, seed)
+        assert np.array_equal(to_host(t), oracle.permutation(n, seed))
+    with pytest.raises(tg.TroveError):
+        tg.fill_run_indices(t, 31, 0)
+
+
 def test_copy_host(cuda):
     torch = cuda
     for n, width, pinned in [(1, 12, False), (100003, 12, True), ((96 << 20) // 28 + 5, 28, True)]:

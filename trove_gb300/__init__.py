@@ -109,6 +109,8 @@ _SIGNATURES = {
                                         ctypes.c_void_p]),
     "trv_fill_uniform_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                                   ctypes.c_void_p]),
+    "trv_fill_run_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_fill_permutation": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p]),
     "trv_copy_host": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32]),
     "trv_batch_create": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.POINTER(BatchOptions),
                                           ctypes.POINTER(ctypes.c_void_p)]),
@@ -267,8 +269,18 @@ def fill_uniform_indices(idx, n: int, bound: int, seed: int, *, stream=None):
     _check(load().trv_fill_uniform_indices(_addr(idx), n, bound, seed, _stream(stream)), "trv_fill_uniform_indices")
 
 
+def fill_run_indices(idx, n: int, seed: int, *, stream=None):
+    """Run pattern: per aligned chunk of 32, a run (p = 1/2) or 32 uniform draws."""
+    _check(load().trv_fill_run_indices(_addr(idx), n, seed, _stream(stream)), "trv_fill_run_indices")
+
+
+def fill_permutation(idx, n: int, seed: int, *, stream=None):
+    """Seeded Fisher-Yates permutation of 0..n-1 (host-generated, copied in)."""
+    _check(load().trv_fill_permutation(_addr(idx), n, seed, _stream(stream)), "trv_fill_permutation")
+
+
 def copy_host(dst_host, src_host, n: int, width: int):
-    """Host-buffer copy through the device; returns when dst_host is written."""
+    """Host-buffer copy; returns when dst_host is written."""
     _check(load().trv_copy_host(_addr(dst_host), _addr(src_host), n, width), "trv_copy_host")
 
 

@@ -2,10 +2,14 @@
 // and launch shape, then one kernel launch on the caller's stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <mutex>
+#include <new>
 #include <unordered_map>
+#include <utility>
+#include <vector>
 
 #include "autotune.h"
 #include "bulk.h"
@@ -414,6 +418,35 @@ int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint6
     launch_uniform_indices(idx, (long long)n, bound, seed, device_info().sm_count * 8,
                            static_cast<cudaStream_t>(stream));
     return check_launch();
+}
+
+int32_t trv_fill_run_indices(int32_t* idx, uint64_t n, uint64_t seed, void* stream) {
+    if (n == 0) return TRV_OK;
+    if (!idx || n < 32 || n > 0x7FFFFFFFull) return TRV_ERR_INVALID_ARGUMENT;
+    if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
+    launch_run_indices(idx, (long long)n, seed, device_info().sm_count * 8, static_cast<cudaStream_t>(stream));
+    return check_launch();
+}
+
+int32_t trv_fill_permutation(int32_t* idx, uint64_t n, uint64_t seed, void* stream) {
+    if (n == 0) return TRV_OK;
+    if (!idx || n > 0x7FFFFFFFull) return TRV_ERR_INVALID_ARGUMENT;
+    if (!aligned(idx, 4)) return TRV_ERR_MISALIGNED;
+    // Fisher-Yates from the top: step i (i = n .. 2) swaps slot i - 1 with a
+    // slot drawn from word i over [0, i).  Inherently sequential, so it runs
+    // on the host and the result is copied once.
+    std::vector<int32_t> h;
+    try {
+        h.resize(n);
+    } catch (const std::bad_alloc&) {
+        return TRV_ERR_OUT_OF_MEMORY;
+    }
+    for (uint64_t i = 0; i < n; ++i) h[i] = int32_t(i);
+    for (uint64_t i = n; i > 1; --i) std::swap(h[i - 1], h[stream_bounded(seed, i, unsigned(i))]);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(idx, h.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // h is freed on return
+    return e == cudaSuccess ? TRV_OK : cuda_fail(e);
 }
 
 int32_t trv_fill_random_u32(uint32_t* dst, uint64_t nwords, uint64_t seed, void* stream) {

@@ -8,39 +8,47 @@
 
 namespace trv {
 
-// ---- seeded input stream (matches the CPU oracle's orc_word) ------------
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
+// ---- seeded input stream (stream_word, flat.h) --------------------------
 __global__ void fill_u32_kernel(unsigned* __restrict__ dst, long long nwords, unsigned long long seed) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nwords; k += stride)
-        dst[k] = (unsigned)(mix64((unsigned long long)k * 0x9E3779B97F4A7C15ull +
-                                  seed * 0xD1B54A32D192ED03ull + 1ull) >>
-                            32);
+        dst[k] = stream_word(seed, (unsigned long long)k);
 }
 
 void launch_fill_u32(unsigned* dst, long long nwords, unsigned long long seed, int grid, cudaStream_t st) {
     fill_u32_kernel<<<grid, 256, 0, st>>>(dst, nwords, seed);
 }
 
-// idx[i] = floor(word(seed, i) * bound / 2^32), the oracle's bounded draw.
+// idx[i] = stream_bounded(seed, i, bound): n indices uniform in [0, bound).
 __global__ void uniform_indices_kernel(int* __restrict__ idx, long long n, unsigned bound, unsigned long long seed) {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-        const unsigned w = (unsigned)(mix64((unsigned long long)k * 0x9E3779B97F4A7C15ull +
-                                            seed * 0xD1B54A32D192ED03ull + 1ull) >>
-                                      32);
-        idx[k] = (int)(((unsigned long long)w * bound) >> 32);
-    }
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+        idx[k] = (int)stream_bounded(seed, (unsigned long long)k, bound);
 }
 
 void launch_uniform_indices(int* idx, long long n, unsigned bound, unsigned long long seed, int grid,
                             cudaStream_t st) {
     uniform_indices_kernel<<<grid, 256, 0, st>>>(idx, n, bound, seed);
+}
+
+// Run pattern over n >= 32 indices: output chunk c (32 aligned outputs) is,
+// when bit 0 of word 2c is set, a run start + 0..31 with start drawn from
+// word 2c + 1 over [0, n - 32]; otherwise 32 independent draws over [0, n)
+// from the stream seed ^ 0x5bd1e995 at the output's own position.  Every
+// output depends only on its chunk, so one thread per output.
+__global__ void run_indices_kernel(int* __restrict__ idx, long long n, unsigned long long seed) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const unsigned long long c = (unsigned long long)k >> 5;
+        if (stream_word(seed, 2 * c) & 1u)
+            idx[k] = (int)(stream_bounded(seed, 2 * c + 1, (unsigned)(n - 31)) + (unsigned)(k & 31));
+        else
+            idx[k] = (int)stream_bounded(seed ^ 0x5bd1e995ull, (unsigned long long)k, (unsigned)n);
+    }
+}
+
+void launch_run_indices(int* idx, long long n, unsigned long long seed, int grid, cudaStream_t st) {
+    run_indices_kernel<<<grid, 256, 0, st>>>(idx, n, seed);
 }
 
 // ---- flat vector copy ----------------------------------------------------
