@@ -9,6 +9,10 @@
   its load and its store when its struct's first word w has w % 625 == 624, so
   about 5 % of 32-struct warp groups run non-converged and take the per-thread
   fallback.  One step = those 32 launches.
+--workload copy12: one contiguous copy of 2^20 structs of 12 B through
+  load/store_warp_contiguous, L2 flushed before every timed launch (the
+  array fits in L2); also reports the L2-resident rate of 100 launches
+  replayed from a CUDA graph.
 --workload gather: dst[i] = src[idx[i]] over 2^24 structs for widths
   {8,12,16,24,32,48,64} B and index patterns permutation / runs of 32 /
   identity; one step = those 21 gathers.
@@ -19,8 +23,8 @@
   launch per array is timed beside it.
 
 GB/s counts bytes read + bytes written + index bytes.  Every array is far
-larger than L2 or the step streams far more than L2 (126 MB), so no flush is
-needed between iterations.  Launch shapes come from the library's autotuner,
+larger than L2 or the step streams far more than L2 (129 MB), so no flush is
+needed between iterations (copy12 flushes).  Launch shapes come from the library's autotuner,
 run before the timed region (its cache is saved and reloaded).  `e2e` times the
 same work with pinned host buffers in and out inside the timed region.
 `--impl reference` times the CPU form of the path (the oracle's
@@ -61,7 +65,7 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["trove", "reference"], default="trove")
-    p.add_argument("--workload", choices=["sweep", "gather", "batch", "serve"], default="sweep")
+    p.add_argument("--workload", choices=["sweep", "copy12", "gather", "batch", "serve"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-check", action="store_true")
@@ -114,19 +118,33 @@ def hbm_peak():
 
 
 class Clocks:
-    """nvidia-smi sampled every 100 ms while the timed region runs."""
+    """nvidia-smi sampled every 100 ms while the timed region runs (a region
+    much shorter than that gets no sample: run it for more steps)."""
     QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.skip = 0
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=self.file, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # The sampler takes a moment to start: wait (at most 3 s) for its first
+        # line, so a short timed region is sampled too, and drop what it
+        # recorded before the region began.
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            with open(self.file.name) as f:
+                lines = f.read().splitlines()
+            if lines:
+                self.skip = len(lines)
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
@@ -136,7 +154,7 @@ class Clocks:
         self.file.seek(0)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.file.read().splitlines():
+        for line in self.file.read().splitlines()[self.skip:]:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 7:
                 continue
@@ -550,6 +568,120 @@ class Batch:
                 "batched_vs_per_call": round(self.per_call_ms / self._batch_ms, 3)}
 
 
+COPY12_N = 1 << 20
+FLUSH_BYTES = 256 << 20
+
+
+class Copy12:
+    """The single contiguous copy: 2^20 structs of 3 x uint32, one launch.
+    Its 24 MiB fit in L2, so a 256 MiB buffer is written between timed
+    launches (outside each launch's events) and the value is bytes over the
+    summed launch times: the cold-L2 rate of one launch."""
+    name = "copy12"
+    kernel_timed = True
+    config = {
+        "workload": "contiguous copy: 2^20 structs of 3 x uint32 (12 B), seed 0, one trv_copy launch through "
+                    "load/store_warp_contiguous, 256 threads/block",
+        "structs": COPY12_N, "width": 12,
+        "l2": "L2 flushed (256 MiB write) before every timed launch; value = bytes / summed launch times",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        self.torch, self.tg, self.dev = torch, tg, dev
+        self.src = torch.empty(COPY12_N * 12, dtype=torch.uint8, device=dev)
+        tg.fill_random_u32(self.src, COPY12_N * 3, seed=0)
+        self.dst = torch.empty_like(self.src)
+        self.flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+        self.unroll = 0  # the library's default until tuned
+        self.tuned = {}
+        torch.cuda.synchronize(dev)
+
+    def _launch_ms(self, unroll, reps=7):
+        """Median time of one flushed launch at the given unroll."""
+        torch = self.torch
+        times = []
+        for _ in range(reps):
+            self.flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            self.tg.copy(self.dst, self.src, COPY12_N, 12, path="warp", unroll=unroll)
+            b.record()
+            torch.cuda.synchronize(self.dev)
+            times.append(a.elapsed_time(b))
+        return statistics.median(times)
+
+    def tune(self):
+        """The warp-contiguous path is fixed by the workload; only its unroll
+        (structs per lane) is chosen, by timing each one."""
+        for u in (1, 2, 4, 8):
+            self.tuned[u] = round(self._launch_ms(u) * 1e3, 2)
+        self.unroll = min(self.tuned, key=self.tuned.get)
+
+    def verify(self):
+        self.dst.fill_(SENTINEL)
+        self.tg.copy(self.dst, self.src, COPY12_N, 12, path="warp")
+        if not self.torch.equal(self.dst, self.src):
+            raise SystemExit("bench verification failed: 12 B contiguous copy")
+
+    def bytes_per_step(self):
+        return 2 * COPY12_N * 12
+
+    def launches_per_step(self):
+        return 1
+
+    def step(self, stream, events):
+        with self.torch.cuda.stream(stream):
+            self.flush.fill_(1)
+        launch_with_events(self.torch, stream, events, "copy_warp_12B", lambda: self.tg.copy(
+            self.dst, self.src, COPY12_N, 12, path="warp", unroll=self.unroll, stream=stream))
+
+    def kernel_bytes(self, key):
+        return self.bytes_per_step()
+
+    def e2e(self, world, steps):
+        """trv_copy_host on pinned host buffers, one call per step."""
+        torch, tg = self.torch, self.tg
+        h_src = self.src.cpu().pin_memory()
+        h_dst = torch.empty_like(h_src).pin_memory()
+        tg.copy_host(h_dst, h_src, COPY12_N, 12)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            tg.copy_host(h_dst, h_src, COPY12_N, 12)
+        el = reduce_max(time.perf_counter() - t0, world, self.dev)
+        if not torch.equal(h_dst, h_src):
+            raise SystemExit("e2e verification failed")
+        return {"value": round(steps * self.bytes_per_step() * world / el / 1e9, 2), "unit": UNIT,
+                "h2d_bytes_per_step": COPY12_N * 12, "d2h_bytes_per_step": COPY12_N * 12, "steps": steps,
+                "path": "trv_copy_host: pinned host buffers read and written in place by the copy kernel"}
+
+    def extra(self):
+        """L2-resident rate: 100 back-to-back launches replayed from one CUDA
+        graph (no flush), the way a caller chaining small copies sees it."""
+        torch, tg = self.torch, self.tg
+        k = 100
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+            for _ in range(k):
+                tg.copy(self.dst, self.src, COPY12_N, 12, path="warp", unroll=self.unroll, stream=side)
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize(self.dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(side)
+        with torch.cuda.stream(side):
+            g.replay()
+        b.record(side)
+        torch.cuda.synchronize(self.dev)
+        per = a.elapsed_time(b) / k
+        return {"unroll": self.unroll, "us_per_launch_by_unroll": self.tuned,
+                "graph_back_to_back": {"launches": k, "us_per_launch": round(per * 1e3, 2),
+                                       "gbs": round(self.bytes_per_step() / per / 1e6, 1), "l2": "resident"}}
+
+
 SERVE_RATES = [2000, 5000, 10000, 20000, 50000]
 SERVE_WIDTHS = [8, 12, 16, 28, 64]
 SERVE_POOL = 1 << 23
@@ -651,7 +783,7 @@ class Serve:
         return total_bytes, total_ms, stats
 
 
-WORKLOADS = {"sweep": Sweep, "gather": Gather, "batch": Batch, "serve": Serve}
+WORKLOADS = {"sweep": Sweep, "copy12": Copy12, "gather": Gather, "batch": Batch, "serve": Serve}
 
 
 # ---- CPU baseline (the oracle's multithreaded port) ----------------------------
@@ -677,6 +809,15 @@ def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = 
                     done += 2 * n * w
             return done
         desc = "the sweep on a 128 MiB array per width (both APIs), early-exit copy"
+    elif workload == "copy12":
+        n = COPY12_N
+        src = oracle.random_words(n * 3, 0, threads=threads).view(np.uint8)
+        dst = np.zeros_like(src)
+
+        def one():
+            oracle.run_mt(oracle.OP_COPY, dst, src, None, n, 12, threads)
+            return 2 * n * 12
+        desc = "the 12 B copy of 2^20 structs (the whole workload)"
     elif workload == "gather":
         n = 1 << 21
         src = oracle.random_words(n * 16, 0, threads=threads).view(np.uint8)
@@ -833,6 +974,8 @@ def run_trove(args, world, rank, local):
     for _ in range(args.warmup):
         wl.step(stream, None)
     ms, events, clock_info = timed(torch, dev, stream, world, args.steps, lambda ev: wl.step(stream, ev))
+    if getattr(wl, "kernel_timed", False):  # flushes ran between the launches: time the launches alone
+        ms = reduce_max(sum(a.elapsed_time(b) for _, a, b in events), world, dev)
     peak, peak_kind = hbm_peak()
     bps = wl.bytes_per_step()
     value = bps * args.steps * world / (ms / 1e3) / 1e9

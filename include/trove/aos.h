@@ -9,9 +9,10 @@
 // lane i passes p_0 + i.  The tile reads its n*sizeof(T) bytes as m
 // coalesced rounds of a word type U, then transposes rows to columns in
 // registers (transpose.h).  U is the widest of int4 / int2 / int that divides
-// sizeof(T) AND that the tile's start address is aligned to, checked at run
-// time (uniform across the tile, so it costs one branch).  One-word structs
-// and structs of more words than the tile has lanes are read per lane.
+// sizeof(T); when the tile's start address is not aligned to U (checked at
+// run time, uniform across the tile) every lane moves its own struct with
+// the widest words its address allows.  One-word structs and structs of more
+// words than the tile has lanes are read per lane.
 //
 // load(p) / store(v, p) take any pointers.  On a fully converged warp, a
 // broadcast of lane 0's pointer and one __ballot_sync tell whether the
@@ -79,6 +80,11 @@ TROVE_D void tile_store_as(const T& data, T* dst, int lane) {
     }
 }
 
+// Only the widest word's tile schedule is compiled in.  A tile whose start is
+// not aligned to that word (possible when alignof(T) is smaller) moves per
+// lane instead: the same bytes, less coalesced, and no second transposition
+// schedule holding registers in every kernel that uses this path (a second
+// and third schedule raised a 64-byte copy kernel from 32 to 47 registers).
 template <std::size_t n, typename T>
 TROVE_D T contiguous_load(const T* src) {
     if constexpr (sizeof(T) % 4 != 0) {
@@ -86,17 +92,13 @@ TROVE_D T contiguous_load(const T* src) {
     } else {
         typedef typename dismember_type<T>::type Umax;
         const int lane = int(lane_id() & unsigned(n - 1));
-        const std::uintptr_t base = reinterpret_cast<std::uintptr_t>(src - lane);
-        if constexpr (sizeof(Umax) == 16) {
-            if ((base & 15) == 0) return tile_load_as<n, int4>(src, lane);
+        if constexpr (alignof(T) >= sizeof(Umax)) {
+            return tile_load_as<n, Umax>(src, lane);
+        } else {
+            const std::uintptr_t base = reinterpret_cast<std::uintptr_t>(src - lane);
+            if ((base & (sizeof(Umax) - 1)) == 0) return tile_load_as<n, Umax>(src, lane);
+            return divergent_load(src);
         }
-        if constexpr (sizeof(Umax) >= 8) {
-            if ((base & 7) == 0) return tile_load_as<n, int2>(src, lane);
-        }
-        if constexpr (alignof(T) < 4) {
-            if ((base & 3) != 0) return *src;
-        }
-        return tile_load_as<n, int>(src, lane);
     }
 }
 
@@ -107,20 +109,13 @@ TROVE_D void contiguous_store(const T& data, T* dst) {
     } else {
         typedef typename dismember_type<T>::type Umax;
         const int lane = int(lane_id() & unsigned(n - 1));
-        const std::uintptr_t base = reinterpret_cast<std::uintptr_t>(dst - lane);
-        if constexpr (sizeof(Umax) == 16) {
-            if ((base & 15) == 0) return tile_store_as<n, int4>(data, dst, lane);
+        if constexpr (alignof(T) >= sizeof(Umax)) {
+            tile_store_as<n, Umax>(data, dst, lane);
+        } else {
+            const std::uintptr_t base = reinterpret_cast<std::uintptr_t>(dst - lane);
+            if ((base & (sizeof(Umax) - 1)) == 0) return tile_store_as<n, Umax>(data, dst, lane);
+            divergent_store(data, dst);
         }
-        if constexpr (sizeof(Umax) >= 8) {
-            if ((base & 7) == 0) return tile_store_as<n, int2>(data, dst, lane);
-        }
-        if constexpr (alignof(T) < 4) {
-            if ((base & 3) != 0) {
-                *dst = data;
-                return;
-            }
-        }
-        tile_store_as<n, int>(data, dst, lane);
     }
 }
 

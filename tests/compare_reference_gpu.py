@@ -12,6 +12,9 @@ checkout exists and travels with the repository.  This library is called
 through its C ABI, as a user would.  Both sides run the same workloads on the
 same buffers:
 
+* the single 12-byte copy: 2^20 structs, one launch (reference kernel
+  `shfl_copy_3`: load_warp_contiguous + store_warp_contiguous, one struct per
+  thread; this library: trv_copy on the warp-contiguous path);
 * the width sweep: s = 1..16 words, 2 GiB arrays of seeded random words, a
   lane leaving between load and store when its first word w has
   w % 625 == 624 (reference kernel `exit_copy_<s>`: load_warp_contiguous /
@@ -49,7 +52,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "sweep", "gather"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather"], default="all")
     args = ap.parse_args()
 
     import torch
@@ -90,6 +93,33 @@ def main():
     d_own = torch.empty_like(d_ref)
     torch.cuda.synchronize(dev)
 
+    if args.part in ("all", "copy12"):
+        n, w = 1 << 20, 12
+        ps, pr = ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(d_ref.data_ptr())
+
+        def ref_copy():
+            cubin("shfl_copy_3", n // 256, ps, pr)  # one struct per thread, 4096 blocks of 256
+
+        def own_copy(unroll):
+            return lambda: tg.copy(d_own, src, n, w, path="warp", unroll=unroll, stream=stream)
+
+        ref_copy()
+        own_copy(0)()
+        torch.cuda.synchronize(dev)
+        if not torch.equal(d_ref[: n * w], d_own[: n * w]):
+            raise SystemExit("outputs differ: 12 B copy")
+        t_ref = timed(ref_copy)
+        by_unroll = {u: timed(own_copy(u)) for u in (1, 2, 4, 8)}  # structs per lane
+        best = min(by_unroll, key=by_unroll.get)
+        t_own = by_unroll[best]
+        row = {"workload": "copy12", "width": w, "structs": n, "reference_us": round(t_ref * 1e3, 2),
+               "this_us": round(t_own * 1e3, 2), "this_unroll": best,
+               "this_us_by_unroll": {u: round(t * 1e3, 2) for u, t in by_unroll.items()},
+               "reference_gbs": round(2 * n * w / t_ref / 1e6, 1),
+               "this_gbs": round(2 * n * w / t_own / 1e6, 1), "ratio": round(t_ref / t_own, 3)}
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+
     if args.part in ("all", "sweep"):
         for s in range(1, 17):
             w = 4 * s
@@ -114,7 +144,6 @@ def main():
             torch.cuda.synchronize(dev)
             if not torch.equal(d_ref, d_own):
                 raise SystemExit(f"outputs differ: width sweep {w} B")
-            skipped = None
             words0 = src[: n * w].view(torch.int32).view(n, s)[:, 0].to(torch.int64) & 0xFFFFFFFF
             skipped = int(((words0 % MODULUS) == (MODULUS - 1)).sum())
             alg = n * w + (n - skipped) * w

@@ -103,6 +103,17 @@ int grid_for(const void* func, long long work_items, int items_per_block, int bl
     return need < 0x7FFFFFFFll ? int(need) : 0x7FFFFFFF;  // one pass per warp
 }
 
+// True (and the grid) when the default launch applies: no grid requested and
+// one 32*unroll-struct chunk per warp fits in a grid of 256-thread blocks.
+bool one_chunk_per_warp(long long n, int unroll, int requested, int* grid) {
+    if (requested != 0) return false;
+    const long long per_block = 256ll * unroll;
+    const long long need = (n + per_block - 1) / per_block;
+    if (need < 1 || need > 0x7FFFFFFFll) return false;
+    *grid = int(need);
+    return true;
+}
+
 int unroll_slot(int unroll) {
     switch (unroll) {
         case 1: return 0;
@@ -259,8 +270,12 @@ int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, cons
     const int slot = unroll_slot(u);
     if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
     const int api = path == TRV_PATH_WARP ? 0 : path == TRV_PATH_BLOCK ? 1 : 2;
-    const CopyKernel& k = ops_for_words(int(width / 4))->copy[api][slot];
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
+    const WidthOps* ops = ops_for_words(int(width / 4));
+    const int ub = ops->built_unroll[slot];
+    int grid = 0;
+    const bool once = one_chunk_per_warp((long long)n, ub, grid_req, &grid);
+    const CopyKernel& k = once ? ops->copy[api][slot] : ops->copy_grid[api][slot];
+    if (!once) grid = grid_for(k.func, (long long)n, 256 * ub, 256, grid_req);
     k.launch(CopyArgs{src, dst, (long long)n, 0u}, grid, 256, st);
     return check_launch();
 }
@@ -291,8 +306,13 @@ int32_t trv_copy_exit_ex(void* dst, const void* src, uint64_t n, uint32_t width,
     }
     const int slot = unroll_slot(u);
     if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
-    const CopyKernel& k = ops_for_words(int(width / 4))->copy_exit[cfg->path == TRV_PATH_WARP ? 0 : 1][slot];
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
+    const int api = cfg->path == TRV_PATH_WARP ? 0 : 1;
+    const WidthOps* ops = ops_for_words(int(width / 4));
+    const int ub = ops->built_unroll[slot];
+    int grid = 0;
+    const bool once = one_chunk_per_warp((long long)n, ub, grid_req, &grid);
+    const CopyKernel& k = once ? ops->copy_exit[api][slot] : ops->copy_exit_grid[api][slot];
+    if (!once) grid = grid_for(k.func, (long long)n, 256 * ub, 256, grid_req);
     k.launch(CopyArgs{src, dst, (long long)n, modulus}, grid, 256, static_cast<cudaStream_t>(stream));
     return check_launch();
 }
@@ -364,7 +384,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
         kp = gather ? &ops->gather[mode][slot] : &ops->scatter[mode][slot];
     }
     const IndexKernel& k = *kp;
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, grid_req);
+    const int grid = grid_for(k.func, (long long)n, 256 * ops->built_unroll[slot], 256, grid_req);
     k.launch(IndexArgs{src, dst, idx, (long long)n, (long long)bound, c.cache_policy}, grid, 256, st);
     return check_launch();
 }
@@ -398,7 +418,7 @@ static int32_t layout_op(bool to_soa, void* dst, const void* src, uint64_t n, ui
     const int u = default_unroll(width);
     const WidthOps* ops = ops_for_words(int(width / 4));
     const CopyKernel& k = to_soa ? ops->aos_to_soa[unroll_slot(u)] : ops->soa_to_aos[unroll_slot(u)];
-    const int grid = grid_for(k.func, (long long)n, 256 * u, 256, 0);
+    const int grid = grid_for(k.func, (long long)n, 256 * ops->built_unroll[unroll_slot(u)], 256, 0);
     k.launch(CopyArgs{src, dst, (long long)n, 0u}, grid, 256, static_cast<cudaStream_t>(stream));
     return check_launch();
 }

@@ -108,35 +108,57 @@ struct WarpGrid {
 // dst[i] = src[i], optionally skipping structs whose first word hits the
 // early-exit predicate (EXIT).  Full chunks are warp-uniform, so their loads
 // run with all 32 lanes; stores after an exit see a partial warp and fall back.
+// The one partial chunk at the end of the array is plain per-lane struct
+// copies: its transposing form would be a second inlined copy of the tile
+// schedule, and every register that copy holds lowers the occupancy of the
+// whole kernel.
+//
+// LOOP = false: the grid has one chunk per warp (the default launch) and the
+// kernel has no loop.  The grid-stride loop's 64-bit induction state costs
+// 4-8 registers per thread, enough to push narrow structs at U = 1 from 24
+// to 32+ registers and below full occupancy (2048 threads per SM), which is
+// where a one-chunk kernel gets its loads in flight.  LOOP = true serves
+// caller-chosen and persistent grids.
 template <int S, int U, int API, bool EXIT>
-__global__ void __launch_bounds__(256)
-copy_kernel(const aos<S>* __restrict__ src, aos<S>* __restrict__ dst, long long n, unsigned modulus) {
-    const WarpGrid g;
+__device__ __forceinline__ void copy_chunk(const aos<S>* __restrict__ src, aos<S>* __restrict__ dst, long long n,
+                                           unsigned modulus, long long base, int lane) {
     constexpr int CH = 32 * U;
-    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
-        if (base + CH <= n) {
-            aos<S> v[U];
+    if (base + CH <= n) {
+        aos<S> v[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) v[u] = load_conv<S, API>(src, base + u * 32 + g.lane);
+        for (int u = 0; u < U; ++u) v[u] = load_conv<S, API>(src, base + u * 32 + lane);
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (!EXIT || !exits(v[u], modulus)) {
-                    if constexpr (EXIT)
-                        store_any<S, API>(dst, base + u * 32 + g.lane, v[u]);
-                    else
-                        store_conv<S, API>(dst, base + u * 32 + g.lane, v[u]);
-                }
-            }
-        } else {
-#pragma unroll 1
-            for (int u = 0; u < U; ++u) {
-                const long long i = base + u * 32 + g.lane;
-                if (i < n) {
-                    const aos<S> v = load_any<S, API>(src, i);
-                    if (!EXIT || !exits(v, modulus)) store_any<S, API>(dst, i, v);
-                }
+        for (int u = 0; u < U; ++u) {
+            if (!EXIT || !exits(v[u], modulus)) {
+                if constexpr (EXIT)
+                    store_any<S, API>(dst, base + u * 32 + lane, v[u]);
+                else
+                    store_conv<S, API>(dst, base + u * 32 + lane, v[u]);
             }
         }
+    } else {
+#pragma unroll 1
+        for (int u = 0; u < U; ++u) {
+            const long long i = base + u * 32 + lane;
+            if (i < n) {
+                const aos<S> v = src[i];
+                if (!EXIT || !exits(v, modulus)) dst[i] = v;
+            }
+        }
+    }
+}
+
+template <int S, int U, int API, bool EXIT, bool LOOP>
+__global__ void __launch_bounds__(256) copy_kernel(const aos<S>* __restrict__ src, aos<S>* __restrict__ dst,
+                                                   long long n, unsigned modulus) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    if constexpr (LOOP) {
+        for (long long base = g.warp * CH; base < n; base += g.warps * CH)
+            copy_chunk<S, U, API, EXIT>(src, dst, n, modulus, base, g.lane);
+    } else {
+        const long long base = g.warp * CH;
+        if (base < n) copy_chunk<S, U, API, EXIT>(src, dst, n, modulus, base, g.lane);
     }
 }
 

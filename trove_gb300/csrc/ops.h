@@ -36,14 +36,22 @@ typedef Kernel<CopyArgs> CopyKernel;
 typedef Kernel<IndexArgs> IndexKernel;
 
 struct WidthOps {
+    // One chunk of 32*unroll structs per warp, no loop: the default grid.
     CopyKernel copy[3][kUnrolls];       // [API_WARP, API_BLOCK, API_DIRECT][unroll]
     CopyKernel copy_exit[2][kUnrolls];  // [API_WARP, API_BLOCK][unroll]
+    // Grid-stride forms of the same, for caller-chosen and persistent grids.
+    CopyKernel copy_grid[3][kUnrolls];
+    CopyKernel copy_exit_grid[2][kUnrolls];
     IndexKernel gather[2][kUnrolls];    // [MODE_COALESCED, MODE_DIRECT][unroll]
     IndexKernel scatter[2][kUnrolls];
     // Row-form kernels: [0] the widest word dividing the width, [1] 4-byte words.
     IndexKernel gather_rows[2][kUnrolls];
     IndexKernel scatter_rows[2][kUnrolls];
     int rows_word_bytes;  // size of the word used by slot [0]
+    // Unroll actually built in each slot (wide structs cap it: a lane keeps
+    // at most 32 words in flight); grids are sized from this, not from the
+    // unroll the caller asked for.
+    int built_unroll[kUnrolls];
     CopyKernel aos_to_soa[kUnrolls];
     CopyKernel soa_to_aos[kUnrolls];
 };

@@ -30,6 +30,10 @@ int resident_blocks(const void* func, int block);
 // overrides.
 int grid_for(const void* func, long long work_items, int items_per_block, int block, int requested);
 
+// True, with the grid, when a launch of one 32*unroll-struct chunk per warp
+// applies (no grid requested, and the grid fits).
+bool one_chunk_per_warp(long long n, int unroll, int requested, int* grid);
+
 int unroll_slot(int unroll);
 int default_unroll(unsigned width);
 

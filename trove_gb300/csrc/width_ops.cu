@@ -12,10 +12,10 @@ namespace {
 
 constexpr int S = TRV_WIDTH;
 
-template <int U, int API, bool EXIT>
+template <int U, int API, bool EXIT, bool LOOP>
 void launch_copy(const CopyArgs& a, int grid, int block, cudaStream_t st) {
-    copy_kernel<S, U, API, EXIT><<<grid, block, 0, st>>>(
-        static_cast<const aos<S>*>(a.src), static_cast<aos<S>*>(a.dst), a.n, a.modulus);
+    copy_kernel<S, U, API, EXIT, LOOP><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src),
+                                                               static_cast<aos<S>*>(a.dst), a.n, a.modulus);
 }
 
 template <int U, int MODE>
@@ -39,10 +39,10 @@ constexpr int unroll_for(int k) {
     return u;
 }
 
-template <int API, bool EXIT, int k>
+template <int API, bool EXIT, bool LOOP, int k>
 CopyKernel copy_entry() {
     constexpr int U = unroll_for(k);
-    return {&launch_copy<U, API, EXIT>, (const void*)&copy_kernel<S, U, API, EXIT>};
+    return {&launch_copy<U, API, EXIT, LOOP>, (const void*)&copy_kernel<S, U, API, EXIT, LOOP>};
 }
 
 // Widest word dividing the struct: 16, 8 or 4 bytes.
@@ -108,12 +108,12 @@ void layout_entries(CopyKernel& to_soa, CopyKernel& to_aos) {
     to_aos = {&launch_soa_to_aos<U>, (const void*)&soa_to_aos_kernel<S, U>};
 }
 
-template <int API, bool EXIT>
+template <int API, bool EXIT, bool LOOP>
 void fill_copy(CopyKernel (&row)[kUnrolls]) {
-    row[0] = copy_entry<API, EXIT, 0>();
-    row[1] = copy_entry<API, EXIT, 1>();
-    row[2] = copy_entry<API, EXIT, 2>();
-    row[3] = copy_entry<API, EXIT, 3>();
+    row[0] = copy_entry<API, EXIT, LOOP, 0>();
+    row[1] = copy_entry<API, EXIT, LOOP, 1>();
+    row[2] = copy_entry<API, EXIT, LOOP, 2>();
+    row[3] = copy_entry<API, EXIT, LOOP, 3>();
 }
 
 template <int MODE, int k>
@@ -142,16 +142,22 @@ void fill_index(IndexKernel (&g)[kUnrolls], IndexKernel (&s)[kUnrolls]) {
 
 WidthOps make_ops() {
     WidthOps ops;
-    fill_copy<API_WARP, false>(ops.copy[API_WARP]);
-    fill_copy<API_BLOCK, false>(ops.copy[API_BLOCK]);
-    fill_copy<API_DIRECT, false>(ops.copy[API_DIRECT]);
-    fill_copy<API_WARP, true>(ops.copy_exit[API_WARP]);
-    fill_copy<API_BLOCK, true>(ops.copy_exit[API_BLOCK]);
+    fill_copy<API_WARP, false, false>(ops.copy[API_WARP]);
+    fill_copy<API_BLOCK, false, false>(ops.copy[API_BLOCK]);
+    fill_copy<API_DIRECT, false, false>(ops.copy[API_DIRECT]);
+    fill_copy<API_WARP, true, false>(ops.copy_exit[API_WARP]);
+    fill_copy<API_BLOCK, true, false>(ops.copy_exit[API_BLOCK]);
+    fill_copy<API_WARP, false, true>(ops.copy_grid[API_WARP]);
+    fill_copy<API_BLOCK, false, true>(ops.copy_grid[API_BLOCK]);
+    fill_copy<API_DIRECT, false, true>(ops.copy_grid[API_DIRECT]);
+    fill_copy<API_WARP, true, true>(ops.copy_exit_grid[API_WARP]);
+    fill_copy<API_BLOCK, true, true>(ops.copy_exit_grid[API_BLOCK]);
     fill_index<MODE_COALESCED>(ops.gather[MODE_COALESCED], ops.scatter[MODE_COALESCED]);
     fill_index<MODE_DIRECT>(ops.gather[MODE_DIRECT], ops.scatter[MODE_DIRECT]);
     fill_rows<typename word_of<kWideWord>::type>(ops.gather_rows[0], ops.scatter_rows[0]);
     fill_rows<unsigned>(ops.gather_rows[1], ops.scatter_rows[1]);
     ops.rows_word_bytes = kWideWord;
+    for (int k = 0; k < kUnrolls; ++k) ops.built_unroll[k] = unroll_for(k);
     layout_entries<0>(ops.aos_to_soa[0], ops.soa_to_aos[0]);
     layout_entries<1>(ops.aos_to_soa[1], ops.soa_to_aos[1]);
     layout_entries<2>(ops.aos_to_soa[2], ops.soa_to_aos[2]);
