@@ -992,8 +992,10 @@ def run_trove(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
         total, el, desc = cpu_sample(args.workload, os.cpu_count() or 1, args.cpu_seconds)
+        total1, el1, desc1 = cpu_sample(args.workload, 1, 0, steps=1)
         cpu = {"value": round(total / el / 1e9, 2), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": desc}
+               "sample": desc,
+               "single_thread": {"value": round(total1 / el1 / 1e9, 2), "unit": UNIT, "cores": 1, "sample": desc1}}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
