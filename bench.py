@@ -15,7 +15,8 @@
   replayed from a CUDA graph.
 --workload gather: dst[i] = src[idx[i]] over 2^24 structs for widths
   {8,12,16,24,32,48,64} B and index patterns permutation / runs of 32 /
-  identity; one step = those 21 gathers.
+  identity; one step = those 21 gathers, L2 flushed before each (their
+  sources are near L2's size), value from the summed gather times.
 --workload batch: 4096 arrays, lengths log-uniform in [2^10, 2^22] structs,
   widths uniform from {4,12,20,36,64} B, 50 % copy / 40 % gather (uniform
   indices) / 10 % scatter (permutation); one step = the whole batch as one
@@ -24,7 +25,7 @@
 
 GB/s counts bytes read + bytes written + index bytes.  Every array is far
 larger than L2 or the step streams far more than L2 (129 MB), so no flush is
-needed between iterations (copy12 flushes).  Launch shapes come from the library's autotuner,
+needed between iterations (copy12 and gather flush).  Launch shapes come from the library's autotuner,
 run before the timed region (its cache is saved and reloaded).  `e2e` times the
 same work with pinned host buffers in and out inside the timed region.
 `--impl reference` times the CPU form of the path (the oracle's
@@ -57,6 +58,8 @@ GATHER_WIDTHS = [8, 12, 16, 24, 32, 48, 64]
 GATHER_PATTERNS = ["perm", "runs", "identity"]
 BATCH_COUNT = 4096
 BATCH_WIDTHS = [4, 12, 20, 36, 64]
+COPY12_N = 1 << 20
+FLUSH_BYTES = 256 << 20  # written between timed launches whose working set would sit in L2
 
 
 def parse():
@@ -339,12 +342,17 @@ class Sweep:
 
 
 class Gather:
+    """21 gathers per step.  Their sources (128 MiB-1 GiB) are near L2's size
+    and overlap from one gather to the next, and a gather may leave source
+    lines persisting in L2, so L2 is flushed before every gather (outside
+    its events) and the value is bytes over the summed gather times."""
     name = "gather"
+    kernel_timed = True
     config = {
         "workload": "random gather dst[i]=src[idx[i]], 2^24 structs, widths 8-64 B, "
                     "idx = permutation / runs of 32 (p=0.5) / identity",
         "structs": GATHER_N, "widths": GATHER_WIDTHS, "patterns": GATHER_PATTERNS,
-        "l2": "each step streams 21 gathers over 0.3-2 GB arrays, no flush",
+        "l2": "L2 flushed (256 MiB write) before every gather; value = bytes / summed gather times",
         "parallelism": "replicas",
     }
 
@@ -358,6 +366,7 @@ class Gather:
         tg.fill_permutation(self.idx["perm"], n, 1)
         tg.fill_run_indices(self.idx["runs"], n, 2)
         self.idx["identity"].copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        self.flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
         torch.cuda.synchronize(dev)
         self.tuned = {}
 
@@ -387,6 +396,8 @@ class Gather:
     def step(self, stream, events):
         for w in GATHER_WIDTHS:
             for p in GATHER_PATTERNS:
+                with self.torch.cuda.stream(stream):
+                    self.flush.fill_(1)
                 launch_with_events(self.torch, stream, events, f"gather_{p}_{w}B", lambda: self.tg.gather(
                     self.dst, self.src, GATHER_N, self.idx[p], GATHER_N, w, stream=stream))
 
@@ -566,10 +577,6 @@ class Batch:
                              "value": round(bps / self.per_call_ms / 1e6, 2), "unit": UNIT,
                              "launches_per_step": BATCH_COUNT},
                 "batched_vs_per_call": round(self.per_call_ms / self._batch_ms, 3)}
-
-
-COPY12_N = 1 << 20
-FLUSH_BYTES = 256 << 20
 
 
 class Copy12:

@@ -131,6 +131,30 @@ def test_gather(cuda, width):
                     assert np.array_equal(to_host(dst), expect), (width, n, name, path, unroll)
 
 
+@pytest.mark.parametrize("width", [4, 8, 12, 24, 64, 100])
+def test_row_form_cache_policies(cuda, width):
+    """Every cache policy of the row-form gather / scatter moves the same
+    bytes as the oracle."""
+    torch = cuda
+    n = 65536 + 17
+    src_h = oracle.random_structs(n, width, seed=width + 3)
+    src = to_dev(torch, src_h)
+    init = np.full(n * width, SENTINEL, np.uint8)
+    sets = index_sets(n, seed=width)
+    for policy in range(4):
+        for name, idx_h in sets.items():
+            idx = torch.from_numpy(idx_h).cuda()
+            dst = to_dev(torch, init)
+            tg.gather(dst, src, n, idx, n, width, path="warp", policy=policy)
+            assert np.array_equal(to_host(dst), oracle.gather(init, src_h, idx_h, n, width)), (policy, name)
+        perm_h = sets["perm"]
+        dst = to_dev(torch, init)
+        tg.scatter(dst, n, src, torch.from_numpy(perm_h).cuda(), n, width, path="warp", policy=policy)
+        assert np.array_equal(to_host(dst), oracle.scatter(init, src_h, perm_h, n, width)), policy
+    with pytest.raises(tg.TroveError):
+        tg.gather(dst, src, n, idx, n, width, path="warp", policy=4)
+
+
 @pytest.mark.parametrize("width", [4, 12, 16, 36, 64])
 def test_gather_out_of_range_indices_are_skipped(cuda, width):
     torch = cuda
