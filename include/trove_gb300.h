@@ -72,7 +72,8 @@ typedef struct trv_launch {
     int32_t chunk_bytes;   /* TRV_PATH_BULK: bytes per shared-memory stage, multiple of 16 */
     int32_t cache_policy;  /* gather / scatter, TRV_PATH_WARP: 0 default; 1 streaming index and
                               contiguous side (evict-first); 2 as 1, random side L2-only;
-                              3 as 1, random side kept in L2 (evict-last) */
+                              3 as 1, random side kept in L2 (evict-last); 4 as 1, random-side
+                              loads with a 64-byte L2 prefetch-size hint */
 } trv_launch;
 
 const char* trv_status_string(int32_t status);

@@ -3,13 +3,14 @@
 Not collected by pytest (no test_ prefix): run it directly on a GB300, after
 the library and the harness cubins are built:
 
-    python tests/compare_reference_gpu.py [--out FILE] [--reps N]
+    python tests/compare_reference_gpu.py [--out FILE] [--reps N] [--tune]
 
 The reference's kernels come from oracle/_ref/trove_ref_kernels.cubin, which
 compiles oracle/trove_bench_kernels.cu (the reference's own test-kernel
 patterns) against the reference's headers; it is built where the reference
 checkout exists and travels with the repository.  This library is called
-through its C ABI, as a user would.  Both sides run the same workloads on the
+through its C ABI, as a user would: default launch shapes, or with --tune
+the shapes its autotuner picks for each width.  Both sides run the same workloads on the
 same buffers:
 
 * the single 12-byte copy: 2^20 structs, one launch (reference kernel
@@ -23,7 +24,8 @@ same buffers:
   AoS copy (`direct_copy_<s>`: r[i] = s[i]);
 * the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
   the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
-  library: trv_gather).
+  library: trv_gather), plus the compiler-generated gather
+  (`direct_gather_<s>`: r[i] = s[indices[i]]).
 
 Every pair of outputs is compared bit for bit before anything is timed.
 Timing: CUDA events around each launch on the launching stream, an L2 flush
@@ -53,6 +55,8 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather"], default="all")
+    ap.add_argument("--tune", action="store_true",
+                    help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
 
     import torch
@@ -131,6 +135,9 @@ def main():
             def ref_exit():
                 cubin(f"exit_copy_{s}", grid, ps, pr, ctypes.c_longlong(n), ctypes.c_uint(MODULUS))
 
+            if args.tune:
+                tg.autotune_call(tg.OP_COPY_EXIT_WARP, w, n)
+
             def own_exit():
                 tg.copy_exit(d_own, src, n, w, MODULUS, path="warp", stream=stream)
 
@@ -166,11 +173,16 @@ def main():
         for w in GATHER_WIDTHS:
             s = w // 4
             assert n * w <= SWEEP_BYTES
+            if args.tune:
+                tg.autotune_call(tg.OP_GATHER, w, n)
             for p, ix in idx.items():
                 pi, ps, pr = (ctypes.c_void_p(t.data_ptr()) for t in (ix, src, d_ref))
 
                 def ref_gather():
                     cubin(f"shfl_gather_{s}", n // 256, pi, ps, pr)
+
+                def direct_gather():
+                    cubin(f"direct_gather_{s}", n // 256, pi, ps, pr)
 
                 def own_gather():
                     tg.gather(d_own, src, n, ix, n, w, stream=stream)
@@ -181,17 +193,18 @@ def main():
                 if not torch.equal(d_ref[: n * w], d_own[: n * w]):
                     raise SystemExit(f"outputs differ: gather {w} B {p}")
                 alg = (2 * w + 4) * n
-                t_ref, t_own = timed(ref_gather), timed(own_gather)
+                t_ref, t_own, t_dir = timed(ref_gather), timed(own_gather), timed(direct_gather)
                 row = {"workload": "gather", "width": w, "pattern": p,
                        "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
-                       "ratio": round(t_ref / t_own, 3)}
+                       "ratio": round(t_ref / t_own, 3), "compiler_aos_gather_gbs": round(alg / t_dir / 1e6, 1)}
                 rows.append(row)
                 print(json.dumps(row), flush=True)
 
     tg.check_device()
     if args.out:
         with open(args.out, "w") as f:
-            json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "rows": rows}, f, indent=1)
+            json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "tuned": args.tune, "rows": rows}, f,
+                      indent=1)
 
 
 if __name__ == "__main__":

@@ -250,6 +250,7 @@ scatter_kernel(const aos<S>* __restrict__ src, const int* __restrict__ idx, aos<
 //    sector share sectors, and a sector that stays in L2 is fetched once
 // 2: as 1, and the random side bypasses L1 (L2 only)
 // 3: as 1, and the random side is marked evict-last in L2
+// 4: as 1, and random-side loads carry a 64-byte L2 prefetch-size hint
 __device__ __forceinline__ unsigned long long l2_evict_last_policy() {
     unsigned long long pol;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
@@ -288,8 +289,30 @@ __device__ __forceinline__ void st_hint(unsigned* p, unsigned v, unsigned long l
     asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
 }
 
+// Random-side loads with a 64-byte L2 prefetch-size hint: on a miss L2 is
+// asked for the 64-byte half line holding the word instead of the whole
+// 128-byte line.
+__device__ __forceinline__ uint4 ld_pf64(const uint4* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.L2::64B.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint2 ld_pf64(const uint2* p) {
+    uint2 v;
+    asm volatile("ld.global.nc.L2::64B.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned ld_pf64(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.global.nc.L2::64B.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 template <typename V>
 __device__ __forceinline__ V ld_random(const V* p, int policy, unsigned long long pol) {
+    if (policy == 4) return ld_pf64(p);
     if (policy == 3) return ld_hint(p, pol);
     if (policy == 2) return __ldcg(p);
     return __ldg(p);
