@@ -13,6 +13,8 @@
   load/store_warp_contiguous, L2 flushed before every timed launch (the
   array fits in L2); also reports the L2-resident rate of 100 launches
   replayed from a CUDA graph.
+--workload layout: AoS -> SoA and SoA -> AoS of a 2 GiB array for s = 1..16
+  words (trv_aos_to_soa / trv_soa_to_aos); one step = those 32 launches.
 --workload gather: dst[i] = src[idx[i]] over 2^24 structs for widths
   {8,12,16,24,32,48,64} B and index patterns permutation / runs of 32 /
   identity; one step = those 21 gathers, L2 flushed before each (their
@@ -68,7 +70,7 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["trove", "reference"], default="trove")
-    p.add_argument("--workload", choices=["sweep", "copy12", "gather", "batch", "serve"], default="sweep")
+    p.add_argument("--workload", choices=["sweep", "copy12", "gather", "batch", "serve", "layout"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-check", action="store_true")
@@ -689,6 +691,69 @@ class Copy12:
                                        "gbs": round(self.bytes_per_step() / per / 1e6, 1), "l2": "resident"}}
 
 
+class Layout:
+    """AoS -> SoA -> AoS on 2 GiB arrays of s = 1..16 words: one step is both
+    conversions for every width (32 launches).  The AoS side moves through the
+    device API (warp-contiguous rounds + transpose), the SoA side as s
+    coalesced 32-bit planes."""
+    name = "layout"
+    config = {
+        "workload": "AoS->SoA and SoA->AoS conversion (trv_aos_to_soa / trv_soa_to_aos), s=1..16 x uint32 "
+                    "(4-64 B), 2 GiB arrays",
+        "structs_per_width": {str(s): ARRAY_BYTES // (4 * s) for s in WORDS},
+        "l2": "inputs larger than L2 (2 GiB arrays), no flush",
+        "parallelism": "replicas",
+    }
+
+    def __init__(self, torch, tg, dev, args):
+        self.torch, self.tg, self.dev = torch, tg, dev
+        self.plan = [(s, 4 * s, ARRAY_BYTES // (4 * s)) for s in WORDS]
+        self.aos = torch.empty(ARRAY_BYTES, dtype=torch.uint8, device=dev)
+        tg.fill_random_u32(self.aos, ARRAY_BYTES // 4, seed=7)
+        self.soa = torch.empty_like(self.aos)
+        self.back = torch.empty_like(self.aos)
+        torch.cuda.synchronize(dev)
+
+    def tune(self):
+        pass
+
+    def verify(self):
+        torch, tg = self.torch, self.tg
+        for s, w, n in self.plan:
+            tg.aos_to_soa(self.soa, self.aos, n, w)
+            tg.soa_to_aos(self.back, self.soa, n, w)
+            words = self.aos[: n * w].view(torch.int32).view(n, s)
+            planes = self.soa[: n * w].view(torch.int32).view(s, n)
+            ok = torch.equal(self.back[: n * w], self.aos[: n * w])
+            ok = ok and all(torch.equal(planes[j], words[:, j]) for j in sorted({0, s - 1}))
+            if not ok:
+                raise SystemExit(f"bench verification failed: layout {w} B")
+
+    def bytes_per_step(self):
+        return sum(4 * n * w for s, w, n in self.plan)
+
+    def launches_per_step(self):
+        return 2 * len(self.plan)
+
+    def step(self, stream, events):
+        torch, tg = self.torch, self.tg
+        for s, w, n in self.plan:
+            launch_with_events(torch, stream, events, f"aos_to_soa_{w}B",
+                               lambda: tg.aos_to_soa(self.soa, self.aos, n, w, stream=stream))
+            launch_with_events(torch, stream, events, f"soa_to_aos_{w}B",
+                               lambda: tg.soa_to_aos(self.back, self.soa, n, w, stream=stream))
+
+    def kernel_bytes(self, key):
+        w = int(key.rsplit("_", 1)[1][:-1])
+        return 2 * (ARRAY_BYTES // w) * w
+
+    def e2e(self, world, steps):
+        return None
+
+    def extra(self):
+        return {}
+
+
 SERVE_RATES = [2000, 5000, 10000, 20000, 50000]
 SERVE_WIDTHS = [8, 12, 16, 28, 64]
 SERVE_POOL = 1 << 23
@@ -790,7 +855,7 @@ class Serve:
         return total_bytes, total_ms, stats
 
 
-WORKLOADS = {"sweep": Sweep, "copy12": Copy12, "gather": Gather, "batch": Batch, "serve": Serve}
+WORKLOADS = {"sweep": Sweep, "copy12": Copy12, "gather": Gather, "batch": Batch, "serve": Serve, "layout": Layout}
 
 
 # ---- CPU baseline (the oracle's multithreaded port) ----------------------------
@@ -816,6 +881,20 @@ def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = 
                     done += 2 * n * w
             return done
         desc = "the sweep on a 128 MiB array per width (both APIs), early-exit copy"
+    elif workload == "layout":
+        sample = 128 << 20
+        src = oracle.random_words(sample // 4, 7, threads=threads).view(np.uint8)
+        mid, back = np.zeros_like(src), np.zeros_like(src)
+
+        def one():
+            done = 0
+            for s in WORDS:
+                w, n = 4 * s, sample // (4 * s)
+                oracle.run_mt(oracle.OP_AOS_TO_SOA, mid, src, None, n, w, threads)
+                oracle.run_mt(oracle.OP_SOA_TO_AOS, back, mid, None, n, w, threads)
+                done += 4 * n * w
+            return done
+        desc = "both conversions on a 128 MiB array per width"
     elif workload == "copy12":
         n = COPY12_N
         src = oracle.random_words(n * 3, 0, threads=threads).view(np.uint8)

@@ -150,7 +150,7 @@ def r2c_source(n: int, m: int):
     return lane.reshape(n, m), elem.reshape(n, m)
 
 
-OP_COPY, OP_GATHER, OP_SCATTER, OP_COPY_EXIT = 0, 1, 2, 3
+OP_COPY, OP_GATHER, OP_SCATTER, OP_COPY_EXIT, OP_AOS_TO_SOA, OP_SOA_TO_AOS = 0, 1, 2, 3, 4, 5
 
 
 def run_mt(op: int, dst: np.ndarray, src: np.ndarray, idx, n: int, width: int, threads: int, modulus: int = 0):

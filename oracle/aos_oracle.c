@@ -182,13 +182,27 @@ void orc_aos_to_soa(uint32_t* soa, const uint32_t* aos, uint64_t n, int s) {
 /* ---- multithreaded forms, for the timed CPU baseline --------------------- */
 
 typedef struct {
-    int op; /* 0 copy, 1 gather, 2 scatter, 3 early-exit copy (modulus in idx slot) */
+    int op; /* 0 copy, 1 gather, 2 scatter, 3 early-exit copy (modulus in idx slot),
+               4 AoS -> SoA, 5 SoA -> AoS */
     unsigned char* dst;
     const unsigned char* src;
     const int32_t* idx;
-    uint64_t begin, end;
+    uint64_t begin, end, total;
     uint32_t width;
 } mt_job;
+
+/* Structs [begin, end) of an n-struct array of s words: AoS -> SoA planes
+ * (plane j, word i at soa[j * n + i]) or back. */
+static void layout_range(int to_soa, uint32_t* dst, const uint32_t* src, uint64_t begin, uint64_t end, uint64_t n,
+                         int s) {
+    for (uint64_t i = begin; i < end; ++i)
+        for (int j = 0; j < s; ++j) {
+            if (to_soa)
+                dst[(uint64_t)j * n + i] = src[i * (uint64_t)s + j];
+            else
+                dst[i * (uint64_t)s + j] = src[(uint64_t)j * n + i];
+        }
+}
 
 static void* mt_worker(void* p) {
     mt_job* j = (mt_job*)p;
@@ -198,6 +212,9 @@ static void* mt_worker(void* p) {
     } else if (j->op == 3) {
         orc_copy_exit(j->dst + j->begin * j->width, j->src + j->begin * j->width, cnt, j->width,
                       (uint32_t)(uintptr_t)j->idx);
+    } else if (j->op == 4 || j->op == 5) {
+        layout_range(j->op == 4, (uint32_t*)j->dst, (const uint32_t*)j->src, j->begin, j->end, j->total,
+                     (int)(j->width / 4));
     } else if (j->op == 1) {
         orc_gather(j->dst + j->begin * j->width, j->src, j->idx + j->begin, cnt, j->width);
     } else {
@@ -207,7 +224,8 @@ static void* mt_worker(void* p) {
 }
 
 /* Static split of n structs over `threads` POSIX threads.  For op 3 the
- * early-exit modulus travels in the idx argument's value. */
+ * early-exit modulus travels in the idx argument's value; ops 4 and 5 (the
+ * AoS <-> SoA layouts of aos_oracle's orc_aos_to_soa) need width % 4 == 0. */
 void orc_run_mt(int op, void* dst, const void* src, const int32_t* idx, uint64_t n, uint32_t width,
                 int threads) {
     if (threads < 1) threads = 1;
@@ -220,6 +238,7 @@ void orc_run_mt(int op, void* dst, const void* src, const int32_t* idx, uint64_t
         jobs[t].src = (const unsigned char*)src;
         jobs[t].idx = idx;
         jobs[t].width = width;
+        jobs[t].total = n;
         jobs[t].begin = n * (uint64_t)t / (uint64_t)threads;
         jobs[t].end = n * (uint64_t)(t + 1) / (uint64_t)threads;
         pthread_create(&th[t], NULL, mt_worker, &jobs[t]);

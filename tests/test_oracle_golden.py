@@ -122,3 +122,15 @@ def test_multithreaded_forms_agree():
         dst = np.zeros(n * w, np.uint8)
         oracle.run_mt(op, dst, src, idx if op else None, n, w, 7)
         assert np.array_equal(dst, expect)
+
+
+def test_multithreaded_layouts_agree():
+    n, w = 10007, 28
+    s = w // 4
+    src = oracle.random_structs(n, w, 5)
+    soa = np.zeros(n * w, np.uint8)
+    oracle.run_mt(oracle.OP_AOS_TO_SOA, soa, src, None, n, w, 7)
+    assert np.array_equal(soa.view(np.uint32), oracle.aos_to_soa(src, n, s))
+    back = np.zeros(n * w, np.uint8)
+    oracle.run_mt(oracle.OP_SOA_TO_AOS, back, soa, None, n, w, 5)
+    assert np.array_equal(back, src.reshape(-1))
