@@ -712,10 +712,16 @@ class Layout:
         tg.fill_random_u32(self.aos, ARRAY_BYTES // 4, seed=7)
         self.soa = torch.empty_like(self.aos)
         self.back = torch.empty_like(self.aos)
+        self.tuned = {}
         torch.cuda.synchronize(dev)
 
     def tune(self):
-        pass
+        tg = self.tg
+        for s, w, n in self.plan:
+            for op, name in ((tg.OP_AOS_TO_SOA, "aos_to_soa"), (tg.OP_SOA_TO_AOS, "soa_to_aos")):
+                if tg.autotune_lookup(tg.SCOPE_CALL, op, w, n) is None:
+                    tg.autotune_call(op, w, n)
+                self.tuned[f"{name}_{w}B"] = tg.autotune_lookup(tg.SCOPE_CALL, op, w, n)[0].unroll
 
     def verify(self):
         torch, tg = self.torch, self.tg
@@ -751,7 +757,7 @@ class Layout:
         return None
 
     def extra(self):
-        return {}
+        return {"tuned_unroll": self.tuned}
 
 
 SERVE_RATES = [2000, 5000, 10000, 20000, 50000]

@@ -152,6 +152,13 @@ int32_t trv_scatter_ex(void* dst, uint64_t dst_n, const void* src, const int32_t
  * the conversion kernels users of it write by hand. */
 int32_t trv_aos_to_soa(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, void* stream);
 int32_t trv_soa_to_aos(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, void* stream);
+/* The same with an explicit unroll / grid (cfg->path is ignored; unroll 0:
+ * the autotuner's choice for TRV_OP_AOS_TO_SOA / TRV_OP_SOA_TO_AOS, else a
+ * width rule). */
+int32_t trv_aos_to_soa_ex(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, const trv_launch* cfg,
+                          void* stream);
+int32_t trv_soa_to_aos_ex(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, const trv_launch* cfg,
+                          void* stream);
 
 /* Synthetic inputs: dst[k] = word k of the seeded splitmix64 stream (the same
  * stream the CPU oracle generates).  No reference counterpart. */
@@ -185,9 +192,12 @@ typedef enum trv_op {
     TRV_OP_COPY = 0,
     TRV_OP_GATHER = 1,
     TRV_OP_SCATTER = 2,
-    /* autotuner keys only: the early-exit copy through each device-API path */
+    /* autotuner keys only: the early-exit copy through each device-API path,
+       and the two layout conversions */
     TRV_OP_COPY_EXIT_WARP = 3,
-    TRV_OP_COPY_EXIT_BLOCK = 4
+    TRV_OP_COPY_EXIT_BLOCK = 4,
+    TRV_OP_AOS_TO_SOA = 5,
+    TRV_OP_SOA_TO_AOS = 6
 } trv_op;
 
 typedef struct trv_task {
@@ -324,8 +334,8 @@ int32_t trv_server_destroy(trv_server* s);
 
 /* Times every candidate launch shape for (op, width, n) on scratch arrays of
  * n structs (uniform random indices for gather / scatter; op may also be
- * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625) and caches
- * the fastest in scope 0. */
+ * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625, or
+ * TRV_OP_AOS_TO_SOA / TRV_OP_SOA_TO_AOS) and caches the fastest in scope 0. */
 int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream);
 /* Times tile sizes for each (op, width, bucket) group of the given tasks,
  * running each group alone as a batch, and caches the fastest in scope 1.

@@ -170,7 +170,7 @@ def test_autotune_on_gpu(cuda, tmp_path):
     torch = cuda
     tg.autotune_clear()
     n, w = 1 << 18, 12
-    for op in (tg.OP_COPY, tg.OP_GATHER, 3, 4):
+    for op in (tg.OP_COPY, tg.OP_GATHER, 3, 4, tg.OP_AOS_TO_SOA, tg.OP_SOA_TO_AOS):
         tg.autotune_call(op, w, n)
         assert tg.autotune_lookup(tg.SCOPE_CALL, op, w, n) is not None, op
     src_h = oracle.random_structs(n, w, seed=1)
@@ -187,6 +187,13 @@ def test_autotune_on_gpu(cuda, tmp_path):
     assert np.array_equal(dst.cpu().numpy(), src_h.reshape(-1))
     assert np.array_equal(gd.cpu().numpy(), oracle.gather(np.zeros(n * w, np.uint8), src_h, idx_h, n, w))
     assert np.array_equal(ed.cpu().numpy(), oracle.copy_exit(init, src_h, n, w, 625)[0])
+    soa = torch.zeros_like(src)
+    tg.aos_to_soa(soa, src, n, w)  # unroll from the cache
+    back = torch.zeros_like(src)
+    tg.soa_to_aos(back, soa, n, w)
+    torch.cuda.synchronize()
+    assert np.array_equal(soa.cpu().numpy().view(np.uint32), oracle.aos_to_soa(src_h, n, w // 4))
+    assert np.array_equal(back.cpu().numpy(), src_h.reshape(-1))
     tasks, expect = make_workload(torch, 60, seed=11)
     tg.autotune_batch(tasks)
     reset(tasks)

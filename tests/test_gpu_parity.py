@@ -299,12 +299,13 @@ def test_aos_soa_round_trip(cuda, width):
         soa_expect = oracle.aos_to_soa(aos_h, n, s)
         assert np.array_equal(soa_expect.reshape(s, n), aos_h.view(np.uint32).reshape(n, s).T)
         aos = to_dev(torch, aos_h)
-        soa = torch.empty(n * width, dtype=torch.uint8, device="cuda")
-        tg.aos_to_soa(soa, aos, n, width)
-        assert np.array_equal(to_host(soa).view(np.uint32), soa_expect), (width, n)
-        back = torch.zeros_like(aos)
-        tg.soa_to_aos(back, soa, n, width)
-        assert np.array_equal(to_host(back), aos_h.reshape(-1)), (width, n)
+        for unroll, grid in [(0, 0), (1, 0), (2, 0), (4, 0), (8, 0), (2, -1), (1, 7)]:
+            soa = torch.empty(n * width, dtype=torch.uint8, device="cuda")
+            tg.aos_to_soa(soa, aos, n, width, unroll=unroll, grid=grid)
+            assert np.array_equal(to_host(soa).view(np.uint32), soa_expect), (width, n, unroll, grid)
+            back = torch.zeros_like(aos)
+            tg.soa_to_aos(back, soa, n, width, unroll=unroll, grid=grid)
+            assert np.array_equal(to_host(back), aos_h.reshape(-1)), (width, n, unroll, grid)
 
 
 @pytest.mark.parametrize("width", [68, 96, 128, 132, 200, 256])

@@ -58,6 +58,8 @@ OP_GATHER = 1
 OP_SCATTER = 2
 OP_COPY_EXIT_WARP = 3   # autotuner keys of the early-exit copy
 OP_COPY_EXIT_BLOCK = 4
+OP_AOS_TO_SOA = 5       # autotuner keys of the layout conversions
+OP_SOA_TO_AOS = 6
 SCOPE_CALL = 0
 SCOPE_BATCH = 1
 
@@ -107,6 +109,10 @@ _SIGNATURES = {
                                         ctypes.c_void_p]),
     "trv_soa_to_aos": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                         ctypes.c_void_p]),
+    "trv_aos_to_soa_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.POINTER(Launch), ctypes.c_void_p]),
+    "trv_soa_to_aos_ex": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.POINTER(Launch), ctypes.c_void_p]),
     "trv_fill_uniform_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                                   ctypes.c_void_p]),
     "trv_fill_run_indices": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p]),
@@ -254,14 +260,18 @@ def fill_random_u32(dst, nwords: int, seed: int, *, stream=None):
     _check(load().trv_fill_random_u32(_addr(dst), nwords, seed, _stream(stream)), "trv_fill_random_u32")
 
 
-def aos_to_soa(dst_soa, src_aos, n: int, width: int, *, stream=None):
+def aos_to_soa(dst_soa, src_aos, n: int, width: int, *, unroll: int = 0, grid: int = 0, stream=None):
     """soa[j * n + i] = field j of struct i (32-bit fields)."""
-    _check(load().trv_aos_to_soa(_addr(dst_soa), _addr(src_aos), n, width, _stream(stream)), "trv_aos_to_soa")
+    cfg = Launch(0, int(unroll), 0, int(grid), 0, 0)
+    _check(load().trv_aos_to_soa_ex(_addr(dst_soa), _addr(src_aos), n, width, ctypes.byref(cfg), _stream(stream)),
+           "trv_aos_to_soa")
 
 
-def soa_to_aos(dst_aos, src_soa, n: int, width: int, *, stream=None):
+def soa_to_aos(dst_aos, src_soa, n: int, width: int, *, unroll: int = 0, grid: int = 0, stream=None):
     """Field j of struct i = soa[j * n + i] (32-bit fields)."""
-    _check(load().trv_soa_to_aos(_addr(dst_aos), _addr(src_soa), n, width, _stream(stream)), "trv_soa_to_aos")
+    cfg = Launch(0, int(unroll), 0, int(grid), 0, 0)
+    _check(load().trv_soa_to_aos_ex(_addr(dst_aos), _addr(src_soa), n, width, ctypes.byref(cfg), _stream(stream)),
+           "trv_soa_to_aos")
 
 
 def fill_uniform_indices(idx, n: int, bound: int, seed: int, *, stream=None):

@@ -111,10 +111,11 @@ using namespace trv;
 extern "C" {
 
 int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) {
-    if (op < TRV_OP_COPY || op > TRV_OP_COPY_EXIT_BLOCK || width == 0 || n == 0 || n > (uint64_t(1) << 40) / width)
+    if (op < TRV_OP_COPY || op > TRV_OP_SOA_TO_AOS || width == 0 || n == 0 || n > (uint64_t(1) << 40) / width)
         return TRV_ERR_INVALID_ARGUMENT;
     const bool exit_op = op == TRV_OP_COPY_EXIT_WARP || op == TRV_OP_COPY_EXIT_BLOCK;
-    if (exit_op && (width % 4 != 0 || width > 64)) return TRV_ERR_UNSUPPORTED;
+    const bool layout_op = op == TRV_OP_AOS_TO_SOA || op == TRV_OP_SOA_TO_AOS;
+    if ((exit_op || layout_op) && (width % 4 != 0 || width > 64)) return TRV_ERR_UNSUPPORTED;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Scratch s;
     const size_t bytes = size_t(n) * width;
@@ -134,6 +135,8 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     if (exit_op) {
         const int path = op == TRV_OP_COPY_EXIT_WARP ? TRV_PATH_WARP : TRV_PATH_BLOCK;
         for (int u : {1, 2, 4, 8}) cands.push_back({path, u, 0, 0, 0, 0});
+    } else if (layout_op) {
+        for (int u : {1, 2, 4, 8}) cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, 0});
     } else if (op == TRV_OP_COPY) {
         for (int chunk : {16 << 10, 24 << 10}) cands.push_back({TRV_PATH_BULK, 0, 0, 0, chunk, 0});
         for (int u : {2, 4, 8}) cands.push_back({TRV_PATH_VECTOR, u, 0, 0, 0, 0});
@@ -151,6 +154,8 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     for (const trv_launch& c : cands) {
         auto run = [&]() -> int {
             if (exit_op) return trv_copy_exit_ex(s.dst, s.src, n, width, 625u, &c, stream);
+            if (op == TRV_OP_AOS_TO_SOA) return trv_aos_to_soa_ex(s.dst, s.src, n, width, &c, stream);
+            if (op == TRV_OP_SOA_TO_AOS) return trv_soa_to_aos_ex(s.dst, s.src, n, width, &c, stream);
             if (op == TRV_OP_COPY) return trv_copy_ex(s.dst, s.src, n, width, &c, stream);
             if (op == TRV_OP_GATHER) return trv_gather_ex(s.dst, s.src, n, s.idx, n, width, &c, stream);
             return trv_scatter_ex(s.dst, n, s.src, s.idx, n, width, &c, stream);

@@ -409,26 +409,55 @@ int32_t trv_scatter(void* dst, uint64_t dst_n, const void* src, const int32_t* i
     return index_op(false, dst, src, dst_n, idx, n, width, nullptr, stream);
 }
 
-static int32_t layout_op(bool to_soa, void* dst, const void* src, uint64_t n, uint32_t width, void* stream) {
+static int32_t layout_op(bool to_soa, void* dst, const void* src, uint64_t n, uint32_t width, const trv_launch* cfg,
+                         void* stream) {
     if (!size_ok(n, width)) return TRV_ERR_INVALID_ARGUMENT;
     if (n == 0) return TRV_OK;
     if (!dst || !src) return TRV_ERR_INVALID_ARGUMENT;
     if (!struct_width(width)) return TRV_ERR_UNSUPPORTED;
     if (!aligned(dst, 4) || !aligned(src, 4)) return TRV_ERR_MISALIGNED;
-    const int u = default_unroll(width);
+    if (cfg && cfg->block_threads != 0 && cfg->block_threads != 256) return TRV_ERR_UNSUPPORTED;
+    int u = cfg ? cfg->unroll : 0;
+    int grid_req = cfg ? cfg->grid_blocks : 0;
+    if (u == 0) {
+        TuneChoice t;
+        if (tune_lookup(TuneKey{SCOPE_CALL, to_soa ? TRV_OP_AOS_TO_SOA : TRV_OP_SOA_TO_AOS, int(width), len_bucket(n)},
+                        &t)) {
+            u = t.unroll;
+            if (grid_req == 0) grid_req = t.grid;
+        } else {
+            u = default_unroll(width);
+        }
+    }
+    const int slot = unroll_slot(u);
+    if (slot < 0) return TRV_ERR_INVALID_ARGUMENT;
     const WidthOps* ops = ops_for_words(int(width / 4));
-    const CopyKernel& k = to_soa ? ops->aos_to_soa[unroll_slot(u)] : ops->soa_to_aos[unroll_slot(u)];
-    const int grid = grid_for(k.func, (long long)n, 256 * ops->built_unroll[unroll_slot(u)], 256, 0);
+    const int ub = ops->built_unroll[slot];
+    int grid = 0;
+    const bool once = one_chunk_per_warp((long long)n, ub, grid_req, &grid);
+    const CopyKernel& k = once ? (to_soa ? ops->aos_to_soa[slot] : ops->soa_to_aos[slot])
+                               : (to_soa ? ops->aos_to_soa_grid[slot] : ops->soa_to_aos_grid[slot]);
+    if (!once) grid = grid_for(k.func, (long long)n, 256 * ub, 256, grid_req);
     k.launch(CopyArgs{src, dst, (long long)n, 0u}, grid, 256, static_cast<cudaStream_t>(stream));
     return check_launch();
 }
 
 int32_t trv_aos_to_soa(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, void* stream) {
-    return layout_op(true, dst_soa, src_aos, n, width, stream);
+    return layout_op(true, dst_soa, src_aos, n, width, nullptr, stream);
 }
 
 int32_t trv_soa_to_aos(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, void* stream) {
-    return layout_op(false, dst_aos, src_soa, n, width, stream);
+    return layout_op(false, dst_aos, src_soa, n, width, nullptr, stream);
+}
+
+int32_t trv_aos_to_soa_ex(void* dst_soa, const void* src_aos, uint64_t n, uint32_t width, const trv_launch* cfg,
+                          void* stream) {
+    return layout_op(true, dst_soa, src_aos, n, width, cfg, stream);
+}
+
+int32_t trv_soa_to_aos_ex(void* dst_aos, const void* src_soa, uint64_t n, uint32_t width, const trv_launch* cfg,
+                          void* stream) {
+    return layout_op(false, dst_aos, src_soa, n, width, cfg, stream);
 }
 
 int32_t trv_fill_uniform_indices(int32_t* idx, uint64_t n, uint32_t bound, uint64_t seed, void* stream) {

@@ -470,58 +470,82 @@ index_rows_rt_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* 
 // aos[i].word(j) and soa[j * n + i].  The AoS side moves through the device
 // API (load/store_warp_contiguous: coalesced rounds + transpose); the SoA side
 // is S coalesced 32-bit streams, one per field.
+// One chunk of 32*U structs; the partial chunk at the end moves per lane.
 template <int S, int U>
-__global__ void __launch_bounds__(256)
-aos_to_soa_kernel(const aos<S>* __restrict__ src, unsigned* __restrict__ dst, long long n) {
-    const WarpGrid g;
+__device__ __forceinline__ void aos_to_soa_chunk(const aos<S>* __restrict__ src, unsigned* __restrict__ dst,
+                                                 long long n, long long base, int lane) {
     constexpr int CH = 32 * U;
-    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
-        aos<S> v[U];
-        const bool full = base + CH <= n;
+    aos<S> v[U];
+    const bool full = base + CH <= n;
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long i = base + u * 32 + g.lane;
-            if (full)
-                v[u] = trove::load_warp_contiguous(src + i);
-            else if (i < n)
-                v[u] = trove::detail::divergent_load(src + i);
-        }
+    for (int u = 0; u < U; ++u) {
+        const long long i = base + u * 32 + lane;
+        if (full)
+            v[u] = trove::load_warp_contiguous(src + i);
+        else if (i < n)
+            v[u] = src[i];
+    }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long i = base + u * 32 + g.lane;
-            if (!full && i >= n) continue;
-            const trove::detail::regs<unsigned, S> w = trove::detail::to_regs(v[u]);
+    for (int u = 0; u < U; ++u) {
+        const long long i = base + u * 32 + lane;
+        if (!full && i >= n) continue;
+        const trove::detail::regs<unsigned, S> w = trove::detail::to_regs(v[u]);
 #pragma unroll
-            for (int j = 0; j < S; ++j) __stcs(dst + (long long)j * n + i, w.v[j]);
-        }
+        for (int j = 0; j < S; ++j) __stcs(dst + (long long)j * n + i, w.v[j]);
     }
 }
 
 template <int S, int U>
+__device__ __forceinline__ void soa_to_aos_chunk(const unsigned* __restrict__ src, aos<S>* __restrict__ dst,
+                                                 long long n, long long base, int lane) {
+    constexpr int CH = 32 * U;
+    const bool full = base + CH <= n;
+    trove::detail::regs<unsigned, S> w[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const long long i = base + u * 32 + lane;
+        if (full || i < n) {
+#pragma unroll
+            for (int j = 0; j < S; ++j) w[u].v[j] = __ldcs(src + (long long)j * n + i);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const long long i = base + u * 32 + lane;
+        const aos<S> v = trove::detail::from_regs(w[u]);
+        if (full)
+            trove::store_warp_contiguous(v, dst + i);
+        else if (i < n)
+            dst[i] = v;
+    }
+}
+
+// LOOP as for copy_kernel: false = one chunk per warp (the default grid).
+template <int S, int U, bool LOOP>
+__global__ void __launch_bounds__(256)
+aos_to_soa_kernel(const aos<S>* __restrict__ src, unsigned* __restrict__ dst, long long n) {
+    const WarpGrid g;
+    constexpr int CH = 32 * U;
+    if constexpr (LOOP) {
+        for (long long base = g.warp * CH; base < n; base += g.warps * CH)
+            aos_to_soa_chunk<S, U>(src, dst, n, base, g.lane);
+    } else {
+        const long long base = g.warp * CH;
+        if (base < n) aos_to_soa_chunk<S, U>(src, dst, n, base, g.lane);
+    }
+}
+
+template <int S, int U, bool LOOP>
 __global__ void __launch_bounds__(256)
 soa_to_aos_kernel(const unsigned* __restrict__ src, aos<S>* __restrict__ dst, long long n) {
     const WarpGrid g;
     constexpr int CH = 32 * U;
-    for (long long base = g.warp * CH; base < n; base += g.warps * CH) {
-        const bool full = base + CH <= n;
-        trove::detail::regs<unsigned, S> w[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long i = base + u * 32 + g.lane;
-            if (full || i < n) {
-#pragma unroll
-                for (int j = 0; j < S; ++j) w[u].v[j] = __ldcs(src + (long long)j * n + i);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long i = base + u * 32 + g.lane;
-            const aos<S> v = trove::detail::from_regs(w[u]);
-            if (full)
-                trove::store_warp_contiguous(v, dst + i);
-            else if (i < n)
-                trove::detail::divergent_store(v, dst + i);
-        }
+    if constexpr (LOOP) {
+        for (long long base = g.warp * CH; base < n; base += g.warps * CH)
+            soa_to_aos_chunk<S, U>(src, dst, n, base, g.lane);
+    } else {
+        const long long base = g.warp * CH;
+        if (base < n) soa_to_aos_chunk<S, U>(src, dst, n, base, g.lane);
     }
 }
 

@@ -52,8 +52,10 @@ struct WidthOps {
     // at most 32 words in flight); grids are sized from this, not from the
     // unroll the caller asked for.
     int built_unroll[kUnrolls];
-    CopyKernel aos_to_soa[kUnrolls];
+    CopyKernel aos_to_soa[kUnrolls];  // one chunk per warp
     CopyKernel soa_to_aos[kUnrolls];
+    CopyKernel aos_to_soa_grid[kUnrolls];  // grid-stride forms
+    CopyKernel soa_to_aos_grid[kUnrolls];
 };
 
 // Row-form gather / scatter with a run-time word count (rows_rt.cu), for any

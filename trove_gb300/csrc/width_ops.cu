@@ -89,23 +89,23 @@ void fill_rows(IndexKernel (&g)[kUnrolls], IndexKernel (&s)[kUnrolls]) {
     rows_entries<V, 3>(g[3], s[3]);
 }
 
-template <int U>
+template <int U, bool LOOP>
 void launch_aos_to_soa(const CopyArgs& a, int grid, int block, cudaStream_t st) {
-    aos_to_soa_kernel<S, U><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src), static_cast<unsigned*>(a.dst),
-                                                    a.n);
+    aos_to_soa_kernel<S, U, LOOP><<<grid, block, 0, st>>>(static_cast<const aos<S>*>(a.src),
+                                                          static_cast<unsigned*>(a.dst), a.n);
 }
 
-template <int U>
+template <int U, bool LOOP>
 void launch_soa_to_aos(const CopyArgs& a, int grid, int block, cudaStream_t st) {
-    soa_to_aos_kernel<S, U><<<grid, block, 0, st>>>(static_cast<const unsigned*>(a.src), static_cast<aos<S>*>(a.dst),
-                                                    a.n);
+    soa_to_aos_kernel<S, U, LOOP><<<grid, block, 0, st>>>(static_cast<const unsigned*>(a.src),
+                                                          static_cast<aos<S>*>(a.dst), a.n);
 }
 
-template <int k>
+template <int k, bool LOOP>
 void layout_entries(CopyKernel& to_soa, CopyKernel& to_aos) {
     constexpr int U = unroll_for(k);
-    to_soa = {&launch_aos_to_soa<U>, (const void*)&aos_to_soa_kernel<S, U>};
-    to_aos = {&launch_soa_to_aos<U>, (const void*)&soa_to_aos_kernel<S, U>};
+    to_soa = {&launch_aos_to_soa<U, LOOP>, (const void*)&aos_to_soa_kernel<S, U, LOOP>};
+    to_aos = {&launch_soa_to_aos<U, LOOP>, (const void*)&soa_to_aos_kernel<S, U, LOOP>};
 }
 
 template <int API, bool EXIT, bool LOOP>
@@ -158,10 +158,14 @@ WidthOps make_ops() {
     fill_rows<unsigned>(ops.gather_rows[1], ops.scatter_rows[1]);
     ops.rows_word_bytes = kWideWord;
     for (int k = 0; k < kUnrolls; ++k) ops.built_unroll[k] = unroll_for(k);
-    layout_entries<0>(ops.aos_to_soa[0], ops.soa_to_aos[0]);
-    layout_entries<1>(ops.aos_to_soa[1], ops.soa_to_aos[1]);
-    layout_entries<2>(ops.aos_to_soa[2], ops.soa_to_aos[2]);
-    layout_entries<3>(ops.aos_to_soa[3], ops.soa_to_aos[3]);
+    layout_entries<0, false>(ops.aos_to_soa[0], ops.soa_to_aos[0]);
+    layout_entries<1, false>(ops.aos_to_soa[1], ops.soa_to_aos[1]);
+    layout_entries<2, false>(ops.aos_to_soa[2], ops.soa_to_aos[2]);
+    layout_entries<3, false>(ops.aos_to_soa[3], ops.soa_to_aos[3]);
+    layout_entries<0, true>(ops.aos_to_soa_grid[0], ops.soa_to_aos_grid[0]);
+    layout_entries<1, true>(ops.aos_to_soa_grid[1], ops.soa_to_aos_grid[1]);
+    layout_entries<2, true>(ops.aos_to_soa_grid[2], ops.soa_to_aos_grid[2]);
+    layout_entries<3, true>(ops.aos_to_soa_grid[3], ops.soa_to_aos_grid[3]);
     return ops;
 }
 
