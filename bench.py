@@ -271,7 +271,8 @@ class Sweep:
         tg.fill_random_u32(self.src, (self.array_bytes + 256) // 4, seed=0)
         if self.array_bytes != ARRAY_BYTES:
             self.config = dict(self.config, structs_per_width={str(s): n for s, _, n in self.plan},
-                               workload=self.config["workload"].replace("2 GiB", f"{args.array_mib} MiB"))
+                               workload=self.config["workload"].replace("2 GiB", f"{args.array_mib} MiB"),
+                               l2=self.config["l2"].replace("2 GiB", f"{args.array_mib} MiB"))
         self.written = {s: n for s, _, n in self.plan}
         self.tuned = {}
 
