@@ -3,15 +3,14 @@
 // (include/trove), so the library's host entry points run exactly the code a
 // user kernel written against that API would run.
 //
-// Work decomposition: a warp owns chunks of 32*U consecutive structs and
-// strides over the array by the grid's warp count; within a chunk lane l owns
-// structs base + u*32 + l (u < U).  All U loads of a chunk are issued before
-// its U stores, which keeps U structs per lane in flight (the memory-level
-// parallelism HBM needs: ~5 MB in flight chip-wide at 6.8 TB/s).  By default
-// the grid has one chunk per warp (measured on GB300 a few percent faster
-// than a persistent grid-stride grid: blocks retire in address order, so the
-// DRAM working set moves through memory as one window); a persistent grid is
-// available through trv_launch.grid_blocks.
+// Work decomposition: a warp owns chunks of 32*U consecutive structs; within
+// a chunk lane l owns structs base + u*32 + l (u < U).  All U loads of a
+// chunk are issued before its U stores, which keeps U structs per lane in
+// flight (the memory-level parallelism HBM needs: ~5 MB in flight chip-wide
+// at 6.8 TB/s).  By default the grid has one chunk per warp and the kernels
+// have no loop (measured on GB300 a few percent faster than a persistent
+// grid-stride grid, and free of the loop's registers); grid-stride forms
+// serve a grid chosen through trv_launch.grid_blocks.
 #pragma once
 
 #include <cuda_runtime.h>
