@@ -53,6 +53,7 @@ METRIC = "AoS copy/gather GB/s & % HBM peak, batched vs per-call (bit-exact); p9
 UNIT = "GB/s"
 ARRAY_BYTES = 1 << 31
 MODULUS = 625
+NOMINAL_HBM_GBS = 8000.0  # HBM3e nominal; the roofline's peak is the measured copy rate
 SENTINEL = 0xA5
 WORDS = list(range(1, 17))
 GATHER_N = 1 << 24
@@ -1097,7 +1098,8 @@ def run_trove(args, world, rank, local):
         "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak, "peak_kind": peak_kind,
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["gbs"], "peak": peak,
                      "unit": "GB/s", "frac": top["frac"], "traffic": traffic,
-                     "bytes_per_launch": top["bytes_per_launch"], "peak_kind": f"of {peak_kind}"},
+                     "bytes_per_launch": top["bytes_per_launch"], "peak_kind": f"of {peak_kind}",
+                     "frac_of_nominal": round(top["gbs"] / NOMINAL_HBM_GBS, 4)},
         "kernels": kernels,
         "e2e": e2e,
         "gpu_launches": args.steps * wl.launches_per_step(),

@@ -24,6 +24,12 @@
  *  - Indices are int32.  Gather/scatter skip an index outside [0, bound):
  *    that output struct (gather) or that source struct (scatter) is left
  *    untouched, so a bad index never faults the GPU.
+ *  - Threads: the stateless calls (copy, gather, scatter, layout, fills) and
+ *    the autotuner cache may be used from any number of host threads at
+ *    once.  A trv_batch handle is used by one thread at a time; a trv_server
+ *    handle may be used from several (it locks internally).
+ *    trv_batch_run_static shares one device array between all callers, so
+ *    its calls must not overlap.
  */
 #ifndef TROVE_GB300_H
 #define TROVE_GB300_H
