@@ -137,6 +137,25 @@ def load_sum(src: np.ndarray, n: int, s: int) -> np.ndarray:
     return out
 
 
+def memory_op(s: int, kind: int, offset: int, stride: int, data: np.ndarray, out_init) -> np.ndarray:
+    """trove/memory.h restated (reference memory.h:136-168 and the
+    warp_load_array / warp_store_array / uncoalesced_store_array recursions
+    above it): warp_load(p, offset, stride)[k] = p[offset + k * stride]
+    (kinds 0 and 1, the volatile overload); warp_store writes
+    p[offset + k * stride] = a[k] (kind 2); uncoalesced_store writes
+    p[k] = a[k], its stride unused (kind 3)."""
+    out = np.array(out_init, np.int32)
+    d = np.asarray(data, np.int32)
+    k = np.arange(s)
+    if kind in (0, 1):
+        out[:s] = d[offset + k * stride]
+    elif kind == 2:
+        out[offset + k * stride] = d[:s]
+    else:
+        out[:s] = d[:s]
+    return out
+
+
 def aos_to_soa(aos: np.ndarray, n: int, s: int) -> np.ndarray:
     out = np.empty(n * s, np.uint32)
     lib().orc_aos_to_soa(_p(out), _p(np.ascontiguousarray(aos).view(np.uint32)), n, s)
@@ -179,6 +198,7 @@ class Emu:
         c.emu_block.argtypes = [i32, i32, v, v, i32]
         c.emu_copy_exit.argtypes = [i32, i32, v, v, ctypes.c_longlong, ctypes.c_uint32]
         c.emu_warp_converged.argtypes = [i32, ctypes.c_uint32, v]
+        c.emu_memory.argtypes = [i32, i32, i32, i32, v, v]
         self.c = c
 
     def transpose(self, direction: str, n: int, m: int, data: np.ndarray) -> np.ndarray:
@@ -229,6 +249,14 @@ class Emu:
     def copy_exit(self, s: int, api: int, src: np.ndarray, n: int, modulus: int, dst_init) -> np.ndarray:
         out = np.array(dst_init, np.int32)
         assert self.c.emu_copy_exit(s, api, _p(np.ascontiguousarray(src)), _p(out), n, modulus) == 0
+        return out
+
+    def memory(self, s: int, kind: int, offset: int, stride: int, data: np.ndarray, out_init) -> np.ndarray:
+        """trove/memory.h: kind 0 warp_load (1: volatile), 2 warp_store,
+        3 uncoalesced_store; data is the source buffer (kinds 0-1) or the
+        s values stored (kinds 2-3)."""
+        out = np.array(out_init, np.int32)
+        assert self.c.emu_memory(s, kind, offset, stride, _p(np.ascontiguousarray(data, np.int32)), _p(out)) == 0
         return out
 
     def warp_converged(self, N: int, active: int) -> np.ndarray:

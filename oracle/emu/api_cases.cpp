@@ -11,8 +11,10 @@
 // warp_converged() check).  `D[i] = S[idx[i]]` is written as two statements
 // because the reference's ref-to-ref assignment does not compile
 // (trove/ptr.h:49-50).  Every entry point returns 0 on success.
+#include <cstring>
 #include <trove/aos.h>
 #include <trove/block.h>
+#include <trove/memory.h>
 #include <trove/ptr.h>
 #include <trove/rotate.h>
 #include <trove/transpose.h>
@@ -210,6 +212,27 @@ struct cases {
     }
 };
 
+// trove/memory.h on the host (the functions are __host__ __device__ and use
+// no lane): kind 0 warp_load, 1 warp_load through a volatile pointer,
+// 2 warp_store of in[0..S) into out, 3 uncoalesced_store of in[0..S).
+template <int S>
+int memory_case(int kind, int offset, int stride, const int* in, int* out) {
+    typedef trove::array<int, S> A;
+    if (kind == 0 || kind == 1) {
+        const A a = kind == 0 ? trove::warp_load<A>(in, offset, stride)
+                              : trove::warp_load<A>(static_cast<const volatile int*>(in), offset, stride);
+        std::memcpy(out, &a, sizeof(A));
+    } else {
+        A a;
+        std::memcpy(&a, in, sizeof(A));
+        if (kind == 2)
+            trove::warp_store(a, out, offset, stride);
+        else
+            trove::uncoalesced_store(a, out, stride);
+    }
+    return 0;
+}
+
 template <typename F, int... S>
 int dispatch_width(int s, F&& f, std::integer_sequence<int, S...>) {
     int rc = 2;
@@ -317,6 +340,11 @@ int emu_block(int s, int write, const int* src, int* dst, int l) {
 int emu_copy_exit(int s, int api, const void* src, void* dst, long long n, unsigned modulus) {
     return dispatch_width(
         s, [&](auto S) { return cases<decltype(S)::value>::copy_exit(api, src, dst, n, modulus); }, widths());
+}
+
+int emu_memory(int s, int kind, int offset, int stride, const int* in, int* out) {
+    return dispatch_width(s, [&](auto S) { return memory_case<decltype(S)::value>(kind, offset, stride, in, out); },
+                          widths());
 }
 
 // warp_converged<N>() seen by each lane of `active`; out[lane] = 0/1, lanes

@@ -1,14 +1,15 @@
 """This repository's device API (include/trove) run on the host lane
 emulator against the golden fixtures recorded from the reference: every
 transposition, copy, known-answer kernel, coalesced_ptr gather/scatter, block
-interface case and warp_converged result must be identical.  CPU only."""
+interface case, warp_converged result and memory.h load/store must be
+identical.  CPU only."""
 import hashlib
 
 import numpy as np
 import pytest
 
 import oracle
-from tests.golden.gen_golden import case_inputs, transpose_cases, transpose_inputs
+from tests.golden.gen_golden import case_inputs, memory_inputs, transpose_cases, transpose_inputs
 
 
 def digest(a):
@@ -81,3 +82,13 @@ def test_misaligned_views(emu, s):
     idx = oracle.permutation(n, 5)
     g = emu.gather(s, src, idx, n)
     assert np.array_equal(g.reshape(n, s), src.reshape(n, s)[idx])
+
+
+def test_memory_functions_match_reference(emu, golden_cases):
+    """warp_load (and its volatile overload), warp_store, uncoalesced_store."""
+    cases = [c for c in golden_cases if c["kind"] == "memory"]
+    assert len(cases) == 19 * 4 * 3
+    for c in cases:
+        data, init = memory_inputs(c)
+        out = emu.memory(c["s"], c["op"], c["offset"], c["stride"], data, init)
+        assert digest(out) == c["sha256"], c

@@ -40,7 +40,7 @@ def oracle_output(case):
 def test_golden_fixture_is_complete(golden_cases, golden_arrays):
     kinds = {c["kind"] for c in golden_cases}
     assert kinds == {"copy", "store_counting", "load_sum", "gather", "scatter", "block", "copy_exit",
-                     "warp_converged"}
+                     "warp_converged", "memory"}
     assert len(golden_arrays) == 2 * len(list(transpose_cases())) + 32
 
 
@@ -134,3 +134,11 @@ def test_multithreaded_layouts_agree():
     back = np.zeros(n * w, np.uint8)
     oracle.run_mt(oracle.OP_SOA_TO_AOS, back, soa, None, n, w, 5)
     assert np.array_equal(back, src.reshape(-1))
+
+
+def test_memory_restatement_matches_reference(golden_cases):
+    from tests.golden.gen_golden import memory_inputs
+    for c in (c for c in golden_cases if c["kind"] == "memory"):
+        data, init = memory_inputs(c)
+        out = oracle.memory_op(c["s"], c["op"], c["offset"], c["stride"], data, init)
+        assert hashlib.sha256(np.ascontiguousarray(out).tobytes()).hexdigest() == c["sha256"], c
