@@ -174,15 +174,11 @@ int copy_bulk(void* dst, const void* src, uint64_t nbytes, int chunk, int grid_r
     return e == cudaSuccess ? TRV_OK : cuda_fail(e);
 }
 
-// Without a tuned entry: the flat vector copy with one pass per warp, which
-// measured fastest on GB300 for every width (7.1 TB/s on 2 GiB arrays, above
-// the TMA bulk path's 6.8 TB/s and the device-API kernels' 6.3-7.2 TB/s).
-int pick_copy_path(const void* dst, const void* src, uint32_t width) {
-    (void)dst;
-    (void)src;
-    (void)width;
-    return TRV_PATH_VECTOR;
-}
+// Copy path without a tuned entry: the flat vector copy, one pass per warp.
+// It needs no alignment beyond the bytes themselves and measured 7.0-7.1 TB/s
+// on 2 GiB arrays at every width on GB300 (TMA bulk 6.8 TB/s; the device-API
+// kernels 6.85-7.18 TB/s once tuned).
+constexpr int kDefaultCopyPath = TRV_PATH_VECTOR;
 
 }  // namespace
 
@@ -256,7 +252,7 @@ int32_t trv_copy_ex(void* dst, const void* src, uint64_t n, uint32_t width, cons
             (t.path != TRV_PATH_WARP || (struct_width(width) && aligned(dst, 4) && aligned(src, 4))))
             c = trv_launch{t.path, t.unroll, 0, t.grid, t.chunk, 0};
         else
-            c.path = pick_copy_path(dst, src, width);
+            c.path = kDefaultCopyPath;
     }
     int path = c.path;
     const int unroll = c.unroll;
