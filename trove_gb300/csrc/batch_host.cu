@@ -54,6 +54,12 @@ int batch_word_log2(const trv_task& t) {
     return 2;
 }
 
+// A batch's plan lives on the device that was current when it was created.
+bool on_batch_device(const trv_batch* b) {
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && dev == b->device;
+}
+
 // Size rule when no tuned tile exists: big enough to amortise the queue
 // step, small enough to balance the tail across 152 SMs.
 int default_tile_bytes(int op) { return op == TRV_OP_COPY ? (128 << 10) : (64 << 10); }
@@ -150,7 +156,7 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
 }
 
 int32_t trv_batch_launch(trv_batch* b, void* stream) {
-    if (!b) return TRV_ERR_INVALID_ARGUMENT;
+    if (!b || !on_batch_device(b)) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (b->exec) {
         const cudaError_t e = cudaGraphLaunch(b->exec, st);
@@ -164,7 +170,7 @@ int32_t trv_batch_launch(trv_batch* b, void* stream) {
 }
 
 int32_t trv_batch_capture(trv_batch* b, void* stream) {
-    if (!b || !stream) return TRV_ERR_INVALID_ARGUMENT;
+    if (!b || !stream || !on_batch_device(b)) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (b->exec) {
         cudaGraphExecDestroy(b->exec);
