@@ -71,6 +71,16 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.soa_to_aos(ok, bad, 5, 12)) == 3
     assert rc_of(lambda: tg.aos_to_soa(0, ok, 5, 12)) == 1
     assert rc_of(lambda: tg.set_l2_fetch_granularity(48)) == 1
+    # layout _ex forms, seeded index generators
+    assert rc_of(lambda: tg.aos_to_soa(ok, ok, 0, 12, unroll=3)) == 0  # n == 0 first
+    assert rc_of(lambda: tg.aos_to_soa(ok, ok, 5, 12, unroll=3)) == 1
+    assert rc_of(lambda: tg.fill_run_indices(ok, 31, 0)) == 1  # runs need n >= 32
+    assert rc_of(lambda: tg.fill_run_indices(bad, 64, 0)) == 3
+    assert rc_of(lambda: tg.fill_run_indices(ok, 1 << 31, 0)) == 1
+    assert rc_of(lambda: tg.fill_permutation(0, 5, 0)) == 1
+    assert rc_of(lambda: tg.fill_permutation(bad, 5, 0)) == 3
+    assert rc_of(lambda: tg.fill_permutation(ok, 0, 0)) == 0
+    assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="warp", policy=5)) == 1
 
 
 def test_error_carries_status_text(trove_lib):
