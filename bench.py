@@ -92,7 +92,12 @@ def dist_setup(args):
     if world > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl" if args.impl == "trove" else "gloo")
+        if args.impl == "trove":
+            import torch
+            torch.cuda.set_device(local)  # before NCCL binds the rank to a device
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group("gloo")
     return world, rank, local
 
 
