@@ -8,7 +8,7 @@
  * tests/block.cu:13-54 are exactly such kernels).  This header is the host
  * boundary that replaces those hand-written kernels: each entry point
  * launches a kernel built on this library's own implementation of that
- * device API (include/trove/*.h, same names and signatures as the
+ * device API (the include/trove headers, same names and signatures as the
  * reference), on one GPU, stream-ordered and asynchronous.
  *
  * Conventions
