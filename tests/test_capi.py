@@ -95,3 +95,28 @@ def test_missing_library_is_an_error(monkeypatch, tmp_path):
     with pytest.raises(RuntimeError, match="not built"):
         mod.load()
     importlib.reload(tg)
+
+
+def test_header_is_plain_c(tmp_path):
+    """The boundary header compiles as C11 with every warning an error, and a
+    C program using it links against the library (no C++ in the ABI)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    prog = tmp_path / "use.c"
+    prog.write_text(
+        "#include <trove_gb300.h>\n"
+        "int main(void) {\n"
+        "    trv_launch cfg = {TRV_PATH_AUTO, 0, 0, 0, 0, 0};\n"
+        "    trv_task t = {TRV_OP_COPY, 12, 0, 0, 0, 0, 0};\n"
+        "    trv_batch* b = 0;\n"
+        "    (void)trv_batch_create(&t, 0, 0, &b);\n"
+        "    return trv_copy_ex(0, 0, 0, 12, &cfg, 0) == TRV_OK ? 0 : 1;\n"
+        "}\n")
+    lib = tg.library_path()
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{HEADER.parent}", str(prog),
+                        f"-L{lib.parent}", "-ltrove_gb300", "-o", str(tmp_path / "use")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
