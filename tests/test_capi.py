@@ -97,7 +97,7 @@ def test_missing_library_is_an_error(monkeypatch, tmp_path):
     importlib.reload(tg)
 
 
-def test_header_is_plain_c(tmp_path):
+def test_header_is_plain_c(trove_lib, tmp_path):
     """The boundary header compiles as C11 with every warning an error, and a
     C program using it links against the library (no C++ in the ABI)."""
     import shutil
