@@ -340,7 +340,8 @@ int32_t trv_server_destroy(trv_server* s);
  * variant.  No reference counterpart. */
 
 /* Times every candidate launch shape for (op, width, n) on scratch arrays of
- * n structs (uniform random indices for gather / scatter; op may also be
+ * n structs, each run after an L2 flush, median of three (uniform random
+ * indices for gather / scatter; op may also be
  * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625, or
  * TRV_OP_AOS_TO_SOA / TRV_OP_SOA_TO_AOS) and caches the fastest in scope 0. */
 int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream);

@@ -197,6 +197,10 @@ def main():
                 row = {"workload": "gather", "width": w, "pattern": p,
                        "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
                        "ratio": round(t_ref / t_own, 3), "compiler_aos_gather_gbs": round(alg / t_dir / 1e6, 1)}
+                choice = tg.autotune_lookup(tg.SCOPE_CALL, tg.OP_GATHER, w, n)
+                if choice is not None:
+                    c = choice[0]
+                    row["tuned"] = {"path": c.path, "unroll": c.unroll, "cache_policy": c.cache_policy}
                 rows.append(row)
                 print(json.dumps(row), flush=True)
 

@@ -12,6 +12,7 @@
 // small JSON array (trv_autotune_save / trv_autotune_load).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -32,10 +33,30 @@ std::map<std::tuple<int, int, int, int>, TuneChoice> g_table;
 
 std::tuple<int, int, int, int> as_tuple(const TuneKey& k) { return std::make_tuple(k.scope, k.op, k.width, k.bucket); }
 
-// Mean milliseconds of `reps` runs of fn after one warm-up run, timed with
-// CUDA events on `st`.  Negative on failure.
+// Written between timed runs so every candidate starts from a cold L2 (the
+// way a large stream of calls meets it): twice the 129 MB L2 of GB300.
+struct L2Flush {
+    void* buf = nullptr;
+    size_t bytes = size_t(256) << 20;
+    L2Flush() {
+        if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            buf = nullptr;
+        }
+    }
+    ~L2Flush() {
+        if (buf) cudaFree(buf);
+    }
+    void run(cudaStream_t st, int value) const {
+        if (buf) cudaMemsetAsync(buf, value, bytes, st);
+    }
+};
+
+// Median milliseconds of `reps` runs of fn after one warm-up run, each run
+// timed alone with CUDA events on `st` after an L2 flush.  Negative on
+// failure.
 template <typename F>
-float time_ms(F&& fn, cudaStream_t st, int reps = 3) {
+float time_ms(F&& fn, cudaStream_t st, const L2Flush& flush, int reps = 3) {
     if (fn() != TRV_OK) return -1.f;
     cudaEvent_t a, b;
     if (cudaEventCreate(&a) != cudaSuccess) return -1.f;
@@ -43,19 +64,25 @@ float time_ms(F&& fn, cudaStream_t st, int reps = 3) {
         cudaEventDestroy(a);
         return -1.f;
     }
-    cudaEventRecord(a, st);
+    std::vector<float> times;
     int rc = TRV_OK;
-    for (int r = 0; r < reps && rc == TRV_OK; ++r) rc = fn();
-    cudaEventRecord(b, st);
-    float ms = -1.f;
-    if (rc == TRV_OK && cudaEventSynchronize(b) == cudaSuccess) {
-        cudaEventElapsedTime(&ms, a, b);
-        ms /= float(reps);
+    for (int r = 0; r < reps && rc == TRV_OK; ++r) {
+        flush.run(st, r);
+        cudaEventRecord(a, st);
+        rc = fn();
+        cudaEventRecord(b, st);
+        float ms = -1.f;
+        if (rc == TRV_OK && cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
+            times.push_back(ms);
+        else
+            rc = TRV_ERR_CUDA;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaGetLastError();
-    return ms;
+    if (rc != TRV_OK || times.empty()) return -1.f;
+    std::sort(times.begin(), times.end());
+    return times[times.size() / 2];
 }
 
 struct Scratch {
@@ -118,6 +145,7 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     if ((exit_op || layout_op) && (width % 4 != 0 || width > 64)) return TRV_ERR_UNSUPPORTED;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     Scratch s;
+    const L2Flush flush;
     const size_t bytes = size_t(n) * width;
     cudaError_t e = cudaMalloc(&s.src, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&s.dst, bytes);
@@ -160,7 +188,7 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
             if (op == TRV_OP_GATHER) return trv_gather_ex(s.dst, s.src, n, s.idx, n, width, &c, stream);
             return trv_scatter_ex(s.dst, n, s.src, s.idx, n, width, &c, stream);
         };
-        const float ms = time_ms(run, st);
+        const float ms = time_ms(run, st, flush);
         if (ms > 0.f && (best < 0.f || ms < best)) {
             best = ms;
             pick = c;
@@ -182,6 +210,7 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
 int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) {
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const L2Flush flush;
     std::map<std::tuple<int, int, int>, std::vector<trv_task>> groups;
     for (uint64_t k = 0; k < count; ++k)
         groups[std::make_tuple(tasks[k].op, int(tasks[k].width), len_bucket(tasks[k].n))].push_back(tasks[k]);
@@ -199,7 +228,7 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
             int rc = trv_batch_create(kv.second.data(), kv.second.size(), &o, &b);
             if (rc != TRV_OK) return rc;
             trv_batch_info(b, nullptr, &bytes);
-            const float ms = time_ms([&]() -> int { return trv_batch_launch(b, stream); }, st);
+            const float ms = time_ms([&]() -> int { return trv_batch_launch(b, stream); }, st, flush);
             trv_batch_destroy(b);
             if (ms > 0.f && (best < 0.f || ms < best)) {
                 best = ms;

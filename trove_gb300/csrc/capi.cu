@@ -319,6 +319,11 @@ int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, ui
     return trv_copy_exit_ex(dst, src, n, width, modulus, &cfg, stream);
 }
 
+// Without a tuned entry, struct gathers and scatters take the row-form path
+// with what the autotuner picked on GB300 for uniform random indices at every
+// width from 8 to 64 bytes: 2 structs per lane up to 8 bytes, else 1;
+// streaming index and contiguous side (policy 1); and from 24 bytes up the
+// gather's random loads with the 64-byte L2 prefetch hint (policy 4).
 static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound, const int32_t* idx, uint64_t n,
                         uint32_t width, const trv_launch* cfg, void* stream) {
     if (!size_ok(n, width) || !size_ok(bound, width)) return TRV_ERR_INVALID_ARGUMENT;
@@ -336,8 +341,10 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
                                            len_bucket(n)},
                                    &t))
             c = trv_launch{t.path, t.unroll, 0, t.grid, 0, t.cache_policy};
+        else if (structs)
+            c = trv_launch{TRV_PATH_WARP, width <= 8 ? 2 : 1, 0, 0, 0, gather && width >= 24 ? 4 : 1};
         else
-            c.path = (structs || wide_words) ? TRV_PATH_WARP : TRV_PATH_VECTOR;
+            c.path = wide_words ? TRV_PATH_WARP : TRV_PATH_VECTOR;
     }
     if (c.cache_policy < 0 || c.cache_policy > 4) return TRV_ERR_INVALID_ARGUMENT;
     const int path = c.path;
