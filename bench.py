@@ -133,7 +133,7 @@ class Clocks:
     much shorter than that gets no sample: run it for more steps)."""
     QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-             "clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_power_cap,clocks.mem")
 
     def __init__(self, index: int):
         self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
@@ -163,7 +163,7 @@ class Clocks:
         self.proc.terminate()
         self.proc.wait()
         self.file.seek(0)
-        sm, smax, reasons = [], [], set()
+        sm, smax, mem, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.file.read().splitlines()[self.skip:]:
             parts = [x.strip() for x in line.split(",")]
@@ -177,9 +177,14 @@ class Clocks:
             for name, val in zip(names, parts[3:7]):
                 if val.lower().startswith("active"):
                     reasons.add(name)
+            if len(parts) > 7:
+                try:
+                    mem.append(float(parts[7]))
+                except ValueError:
+                    pass
         os.unlink(self.file.name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "mem_mhz": statistics.median(mem) if mem else None, "samples": len(sm), "reasons": sorted(reasons)}
 
 
 def timed(torch, dev, stream, world, steps, step_fn, label_events=True):

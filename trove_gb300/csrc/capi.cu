@@ -320,10 +320,10 @@ int32_t trv_copy_exit(void* dst, const void* src, uint64_t n, uint32_t width, ui
 }
 
 // Without a tuned entry, struct gathers and scatters take the row-form path
-// with what the autotuner picked on GB300 for uniform random indices at every
-// width from 8 to 64 bytes: 2 structs per lane up to 8 bytes, else 1;
-// streaming index and contiguous side (policy 1); and from 24 bytes up the
-// gather's random loads with the 64-byte L2 prefetch hint (policy 4).
+// with 2 structs per lane, streaming index and contiguous side, and (gather)
+// random loads with the 64-byte L2 prefetch hint (policy 4): measured on
+// GB300 with L2 flushed, the best or within 1 % of the best at every width
+// from 8 to 64 bytes on permutations, runs of 32 and the identity.
 static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound, const int32_t* idx, uint64_t n,
                         uint32_t width, const trv_launch* cfg, void* stream) {
     if (!size_ok(n, width) || !size_ok(bound, width)) return TRV_ERR_INVALID_ARGUMENT;
@@ -342,7 +342,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
                                    &t))
             c = trv_launch{t.path, t.unroll, 0, t.grid, 0, t.cache_policy};
         else if (structs)
-            c = trv_launch{TRV_PATH_WARP, width <= 8 ? 2 : 1, 0, 0, 0, gather && width >= 24 ? 4 : 1};
+            c = trv_launch{TRV_PATH_WARP, 2, 0, 0, 0, gather ? 4 : 1};
         else
             c.path = wide_words ? TRV_PATH_WARP : TRV_PATH_VECTOR;
     }
