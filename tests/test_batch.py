@@ -62,6 +62,9 @@ def test_batch_argument_errors(trove_lib):
     for bad_path in ["bulk", "warp"]:
         with pytest.raises(tg.TroveError):
             tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path=bad_path)
+    with pytest.raises(tg.TroveError) as e:
+        tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], gather_policy=2)
+    assert e.value.status == 1
 
 
 def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000):
@@ -117,12 +120,13 @@ def check(tasks, expect):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("gather_policy", [0, 1, 4])
 @pytest.mark.parametrize("copy_path", ["vector", "auto"])
 @pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
-def test_batch_matches_oracle(cuda, copy_path, tile_bytes):
+def test_batch_matches_oracle(cuda, copy_path, tile_bytes, gather_policy):
     torch = cuda
     tasks, expect = make_workload(torch, 120, seed=3)
-    b = tg.Batch(tasks, tile_bytes=tile_bytes, copy_path=copy_path)
+    b = tg.Batch(tasks, tile_bytes=tile_bytes, copy_path=copy_path, gather_policy=gather_policy)
     tiles, nbytes = b.info()
     assert tiles > 0 and nbytes > 0
     b.launch()

@@ -216,14 +216,16 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         groups[std::make_tuple(tasks[k].op, int(tasks[k].width), len_bucket(tasks[k].n))].push_back(tasks[k]);
     for (auto& kv : groups) {
         const int op = std::get<0>(kv.first);
-        std::vector<std::pair<int, int>> cands;  // (tile_bytes, blocks per SM)
+        std::vector<std::tuple<int, int, int>> cands;  // (tile_bytes, blocks per SM, gather policy)
         for (int tb : {16 << 10, 64 << 10, 256 << 10, 1 << 20})
-            for (int bps : {2, 4}) cands.push_back({tb, bps});
+            for (int bps : {2, 4})
+                for (int gp : {1, 4})
+                    if (op == TRV_OP_GATHER || gp == 1) cands.push_back({tb, bps, gp});
         float best = -1.f;
-        std::pair<int, int> pick{0, 0};
+        std::tuple<int, int, int> pick{0, 0, 0};
         uint64_t bytes = 0;
         for (const auto& c : cands) {
-            trv_batch_options o{c.first, TRV_PATH_AUTO, 0, c.second};
+            trv_batch_options o{std::get<0>(c), TRV_PATH_AUTO, 0, std::get<1>(c), std::get<2>(c)};
             trv_batch* b = nullptr;
             int rc = trv_batch_create(kv.second.data(), kv.second.size(), &o, &b);
             if (rc != TRV_OK) return rc;
@@ -237,8 +239,9 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         }
         if (best < 0.f) return TRV_ERR_CUDA;
         TuneChoice ch;
-        ch.tile_bytes = pick.first;
-        ch.grid = pick.second;  // blocks per SM of the batch kernel
+        ch.tile_bytes = std::get<0>(pick);
+        ch.grid = std::get<1>(pick);  // blocks per SM of the batch kernel
+        ch.cache_policy = std::get<2>(pick);
         ch.gbs = double(bytes) / (double(best) * 1e6);
         tune_store(TuneKey{SCOPE_BATCH, op, std::get<1>(kv.first), std::get<2>(kv.first)}, ch);
     }

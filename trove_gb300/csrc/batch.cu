@@ -78,7 +78,7 @@ __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned 
 // uniform across the warp, so the guarded shuffles are too.
 template <typename V, int U, int G, bool GATHER>
 __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int* idx, long long bound, long long first,
-                                                long long cnt, int m) {
+                                                long long cnt, int m, bool hint) {
     const int tid = opaque_tid();
     const int lane = tid & 31, warp = tid >> 5;
     const long long end = first + cnt;
@@ -104,8 +104,9 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
                         const int j = q / m;
                         other[u][g] = __shfl_sync(0xFFFFFFFFu, id[u], j);
                         if (other[u][g] >= 0)
-                            val[u][g] = GATHER ? __ldg(src + (long long)other[u][g] * m + (q - j * m))
-                                               : __ldcs(src + (base + u * 32) * m + q);
+                            val[u][g] = !GATHER ? __ldcs(src + (base + u * 32) * m + q)
+                                        : hint  ? ld_pf64(src + (long long)other[u][g] * m + (q - j * m))
+                                                : __ldg(src + (long long)other[u][g] * m + (q - j * m));
                     }
                 }
 #pragma unroll
@@ -128,13 +129,14 @@ __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, 
     const int m = t.words * 4 >> t.word_log2;
     if (t.word_log2 == 4)
         tile_index_rows<uint4, 2, 2, GATHER>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
-                                             t.idx, t.bound, first, cnt, m);
+                                             t.idx, t.bound, first, cnt, m, t.l2_hint != 0);
     else if (t.word_log2 == 3)
         tile_index_rows<uint2, 2, 4, GATHER>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
-                                             t.idx, t.bound, first, cnt, m);
+                                             t.idx, t.bound, first, cnt, m, t.l2_hint != 0);
     else
         tile_index_rows<unsigned, 2, 4, GATHER>(reinterpret_cast<const unsigned*>(t.src),
-                                                reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m);
+                                                reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m,
+                                                t.l2_hint != 0);
 }
 
 // MINB resident blocks per SM: 2 gives each thread 128 registers (no

@@ -16,6 +16,7 @@ struct alignas(16) BatchTask {
     int words;        // struct width / 4
     int tile_structs; // structs per tile, a multiple of 32
     int word_log2;    // gather / scatter: log2 of the word moved per lane (2, 3 or 4)
+    int l2_hint;      // gather: 1 = random loads carry the 64-byte L2 prefetch-size hint
 };
 
 // blocks_per_sm: 2 or 4 (the register budget the kernel was built for).

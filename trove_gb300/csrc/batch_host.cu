@@ -92,6 +92,8 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     if (opt && opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
     if (opt && opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4)
         return TRV_ERR_UNSUPPORTED;
+    if (opt && opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4)
+        return TRV_ERR_INVALID_ARGUMENT;
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
     uint64_t bytes = 0;
@@ -119,6 +121,13 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         d.words = int(t.width / 4);
         d.tile_structs = int(tile);
         d.word_log2 = batch_word_log2(t);
+        // Gather loads: plain unless chosen otherwise.  The hint measured 3 %
+        // slower on the 4096-array workload's uniform-index gathers, most of
+        // whose sources are small enough to be L2-resident.
+        const int gp = (opt && opt->gather_policy) ? opt->gather_policy
+                       : (tuned && c.cache_policy) ? c.cache_policy
+                                                   : 1;
+        d.l2_hint = (t.op == TRV_OP_GATHER && gp == 4) ? 1 : 0;
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
         const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
         bytes += tb;
