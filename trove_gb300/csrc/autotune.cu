@@ -179,7 +179,9 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     }
     float best = -1.f;
     trv_launch pick{};
-    for (const trv_launch& c : cands) {
+    std::vector<float> times(cands.size(), -1.f);
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+        const trv_launch& c = cands[ci];
         auto run = [&]() -> int {
             if (exit_op) return trv_copy_exit_ex(s.dst, s.src, n, width, 625u, &c, stream);
             if (op == TRV_OP_AOS_TO_SOA) return trv_aos_to_soa_ex(s.dst, s.src, n, width, &c, stream);
@@ -189,12 +191,27 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
             return trv_scatter_ex(s.dst, n, s.src, s.idx, n, width, &c, stream);
         };
         const float ms = time_ms(run, st, flush);
+        times[ci] = ms;
         if (ms > 0.f && (best < 0.f || ms < best)) {
             best = ms;
             pick = c;
         }
     }
     if (best < 0.f) return TRV_ERR_CUDA;
+    // Gathers and scatters are tuned on uniform random indices, where unrolls
+    // of the same path and policy often tie; runs and contiguous stretches of
+    // indices gain from more structs per lane, so within 2 % of the best the
+    // largest unroll wins.
+    float pick_ms = best;
+    if (op == TRV_OP_GATHER || op == TRV_OP_SCATTER)
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+            const trv_launch& c = cands[ci];
+            if (times[ci] > 0.f && times[ci] <= best * 1.02f && c.path == pick.path &&
+                c.cache_policy == pick.cache_policy && c.unroll > pick.unroll) {
+                pick = c;
+                pick_ms = times[ci];
+            }
+        }
     TuneChoice ch;
     ch.path = pick.path;
     ch.unroll = pick.unroll;
@@ -202,7 +219,7 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     ch.chunk = pick.chunk_bytes;
     ch.cache_policy = pick.cache_policy;
     const double alg = double(bytes) * 2 + (op == TRV_OP_GATHER || op == TRV_OP_SCATTER ? 4.0 * double(n) : 0.0);
-    ch.gbs = alg / (double(best) * 1e6);
+    ch.gbs = alg / (double(pick_ms) * 1e6);
     tune_store(TuneKey{SCOPE_CALL, op, int(width), len_bucket(n)}, ch);
     return TRV_OK;
 }
