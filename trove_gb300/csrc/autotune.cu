@@ -199,15 +199,16 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     }
     if (best < 0.f) return TRV_ERR_CUDA;
     // Gathers and scatters are tuned on uniform random indices, where unrolls
-    // of the same path and policy often tie; runs and contiguous stretches of
-    // indices gain from more structs per lane, so within 2 % of the best the
-    // largest unroll wins.
+    // of the same path and policy often tie; on runs and contiguous stretches
+    // of indices 2 structs per lane measured best or near best at every width
+    // (1 is slower there, 4-8 slower from 24 bytes up), so within 2 % of the
+    // best an unroll of 2 wins.
     float pick_ms = best;
     if (op == TRV_OP_GATHER || op == TRV_OP_SCATTER)
         for (size_t ci = 0; ci < cands.size(); ++ci) {
             const trv_launch& c = cands[ci];
             if (times[ci] > 0.f && times[ci] <= best * 1.02f && c.path == pick.path &&
-                c.cache_policy == pick.cache_policy && c.unroll > pick.unroll) {
+                c.cache_policy == pick.cache_policy && c.unroll == 2 && pick.unroll != 2) {
                 pick = c;
                 pick_ms = times[ci];
             }
