@@ -234,7 +234,9 @@ TROVE_D void store_warp_contiguous(const T& data, T* dest) {
 
 template <typename T>
 TROVE_D T load(const T* src) {
-    if constexpr (sizeof(T) % 4 == 0) {
+    // A struct of one widest word is one access per lane whether or not the
+    // warp's pointers are consecutive: no vote needed.
+    if constexpr (sizeof(T) % 4 == 0 && sizeof(T) != sizeof(typename detail::dismember_type<T>::type)) {
         if (warp_converged()) {
             if (detail::warp_consecutive(src)) return detail::contiguous_load<WARP_SIZE>(src);
             return detail::warp_gather_load(src);
@@ -245,7 +247,7 @@ TROVE_D T load(const T* src) {
 
 template <typename T>
 TROVE_D void store(const T& data, T* dest) {
-    if constexpr (sizeof(T) % 4 == 0) {
+    if constexpr (sizeof(T) % 4 == 0 && sizeof(T) != sizeof(typename detail::dismember_type<T>::type)) {
         if (warp_converged()) {
             if (detail::warp_consecutive(dest))
                 detail::contiguous_store<WARP_SIZE>(data, dest);
