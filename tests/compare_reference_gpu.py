@@ -22,6 +22,9 @@ same buffers:
   store_warp_contiguous with the warp_converged() fallback; this library:
   trv_copy_exit on the warp-contiguous path), plus the compiler-generated
   AoS copy (`direct_copy_<s>`: r[i] = s[i]);
+* the device-API gather (--part api_gather): the coalesced_ptr gather kernel
+  source `shfl_gather_<s>` built against the reference's headers and against
+  this repository's, widths 4..64 B, the three index patterns;
 * the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
   the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
   library: trv_gather), plus the compiler-generated gather
@@ -54,7 +57,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather"], default="all")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
@@ -201,6 +204,43 @@ def main():
                 if choice is not None:
                     c = choice[0]
                     row["tuned"] = {"path": c.path, "unroll": c.unroll, "cache_policy": c.cache_policy}
+                rows.append(row)
+                print(json.dumps(row), flush=True)
+
+    if args.part in ("all", "api_gather"):
+        # The device API as users meet it: the same coalesced_ptr gather kernel
+        # source built against both header trees.
+        own = oracle.own_cubin()
+        n = GATHER_N
+        idx = {p: torch.empty(n, dtype=torch.int32, device=dev) for p in ("perm", "runs", "identity")}
+        tg.fill_permutation(idx["perm"], n, 1)
+        tg.fill_run_indices(idx["runs"], n, 2)
+        idx["identity"].copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        torch.cuda.synchronize(dev)
+        for s in range(1, 17):
+            w = 4 * s
+            for p, ix in idx.items():
+                a_ref = [ctypes.c_void_p(ix.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                         ctypes.c_void_p(d_ref.data_ptr())]
+                a_own = [ctypes.c_void_p(ix.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                         ctypes.c_void_p(d_own.data_ptr())]
+
+                def ref_api():
+                    cubin(f"shfl_gather_{s}", n // 256, *a_ref)
+
+                def own_api():
+                    own.launch(f"shfl_gather_{s}", n // 256, 256, a_own, stream.cuda_stream)
+
+                ref_api()
+                own_api()
+                torch.cuda.synchronize(dev)
+                if not torch.equal(d_ref[: n * w], d_own[: n * w]):
+                    raise SystemExit(f"outputs differ: device-API gather {w} B {p}")
+                alg = (2 * w + 4) * n
+                t_ref, t_own = timed(ref_api), timed(own_api)
+                row = {"workload": "api_gather", "width": w, "pattern": p,
+                       "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
+                       "ratio": round(t_ref / t_own, 3)}
                 rows.append(row)
                 print(json.dumps(row), flush=True)
 
