@@ -218,7 +218,9 @@ typedef struct trv_task {
 
 typedef struct trv_batch_options {
     int32_t tile_bytes;  /* payload bytes per tile; 0: autotuner cache, else the size rule */
-    int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO or TRV_PATH_VECTOR (flat vector tiles) */
+    int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO (the autotuned choice, else TMA bulk tiles
+                            where source and destination are 16-byte aligned) or
+                            TRV_PATH_VECTOR (flat vector tiles) */
     int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
     int32_t blocks_per_sm; /* 2: 128 registers per thread (0: the autotuned or default choice, 2);
                               4: 64 registers, twice the warps */

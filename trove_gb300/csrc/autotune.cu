@@ -234,16 +234,21 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         groups[std::make_tuple(tasks[k].op, int(tasks[k].width), len_bucket(tasks[k].n))].push_back(tasks[k]);
     for (auto& kv : groups) {
         const int op = std::get<0>(kv.first);
-        std::vector<std::tuple<int, int, int>> cands;  // (tile_bytes, blocks per SM, gather policy)
+        // (tile_bytes, blocks per SM, gather load policy, copy tile path)
+        std::vector<std::tuple<int, int, int, int>> cands;
         for (int tb : {16 << 10, 64 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
                 for (int gp : {1, 4})
-                    if (op == TRV_OP_GATHER || gp == 1) cands.push_back({tb, bps, gp});
+                    for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
+                        if (gp == 4 && op != TRV_OP_GATHER) continue;
+                        if (cpath == TRV_PATH_VECTOR && op != TRV_OP_COPY) continue;
+                        cands.push_back({tb, bps, gp, cpath});
+                    }
         float best = -1.f;
-        std::tuple<int, int, int> pick{0, 0, 0};
+        std::tuple<int, int, int, int> pick{0, 0, 0, 0};
         uint64_t bytes = 0;
         for (const auto& c : cands) {
-            trv_batch_options o{std::get<0>(c), TRV_PATH_AUTO, 0, std::get<1>(c), std::get<2>(c)};
+            trv_batch_options o{std::get<0>(c), std::get<3>(c), 0, std::get<1>(c), std::get<2>(c)};
             trv_batch* b = nullptr;
             int rc = trv_batch_create(kv.second.data(), kv.second.size(), &o, &b);
             if (rc != TRV_OK) return rc;
@@ -260,6 +265,7 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         ch.tile_bytes = std::get<0>(pick);
         ch.grid = std::get<1>(pick);  // blocks per SM of the batch kernel
         ch.cache_policy = std::get<2>(pick);
+        ch.path = std::get<3>(pick);  // copy groups: TRV_PATH_AUTO (TMA tiles) or TRV_PATH_VECTOR
         ch.gbs = double(bytes) / (double(best) * 1e6);
         tune_store(TuneKey{SCOPE_BATCH, op, std::get<1>(kv.first), std::get<2>(kv.first)}, ch);
     }

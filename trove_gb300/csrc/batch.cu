@@ -20,6 +20,7 @@
 #include "batch.h"
 #include "kernels.cuh"
 #include "runtime.h"
+#include "tma.cuh"
 #include "trove_gb300.h"
 
 namespace trv {
@@ -27,6 +28,17 @@ namespace {
 
 constexpr int kBatchBlock = 256;
 constexpr int kWarps = kBatchBlock / 32;
+
+// Copy tiles whose source and destination are 16-byte aligned move through
+// the TMA bulk engine: one thread streams the tile as kBulkChunk pieces
+// through a ring of kBulkStages shared-memory buffers (load, then store of
+// each piece; a stage is refilled once the store that read it has finished).
+// The bytes in flight then come from shared memory, not from registers,
+// which the kernel's gather / scatter movers already use up (2 resident
+// blocks per SM at 128 registers).
+constexpr int kBulkStages = 4;
+constexpr int kBulkChunk = 8 << 10;
+constexpr int kBulkSmem = kBulkStages * kBulkChunk;
 
 // ---- per-tile movers (all warps of the CTA cooperate on one tile) --------
 
@@ -67,6 +79,56 @@ __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned 
         done = nv << 2;
     }
     for (long long b = done + tid; b < nbytes; b += kBatchBlock) d[b] = s[b];
+}
+
+// TMA bulk copy of one tile by the calling thread (thread 0 of the CTA).
+// `seq` numbers the loads this CTA has issued over the whole launch: load k
+// uses stage k % S and completes phase (k / S) & 1 of that stage's
+// mbarrier.  Every wait is bounded; on a timeout the device flag is set, the
+// loads still in flight are drained (bounded) and false is returned.
+__device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long long nbytes, unsigned char* stage,
+                               unsigned long long* bar, unsigned long long& seq, int* flag) {
+    const long long body = nbytes & ~15ll;
+    const long long nchunks = (body + kBulkChunk - 1) / kBulkChunk;
+    auto chunk_bytes = [&](long long c) -> unsigned {
+        const long long off = c * kBulkChunk;
+        return static_cast<unsigned>(body - off < kBulkChunk ? body - off : kBulkChunk);
+    };
+    auto issue = [&](long long c) {
+        const int st = int((seq + (unsigned long long)c) % kBulkStages);
+        mbar_expect_tx(&bar[st], chunk_bytes(c));
+        bulk_load(stage + (size_t)st * kBulkChunk, s + c * kBulkChunk, chunk_bytes(c), &bar[st]);
+    };
+    const long long prologue = nchunks < kBulkStages ? nchunks : kBulkStages;
+    for (long long c = 0; c < prologue; ++c) issue(c);
+    long long issued = prologue;
+    bool ok = true;
+    long long c = 0;
+    for (; c < nchunks; ++c) {
+        const unsigned long long k = seq + (unsigned long long)c;
+        const int st = int(k % kBulkStages);
+        if (!mbar_wait(&bar[st], unsigned((k / kBulkStages) & 1))) {
+            ok = false;
+            break;
+        }
+        fence_proxy_async_shared();
+        bulk_store(d + c * kBulkChunk, stage + (size_t)st * kBulkChunk, chunk_bytes(c));
+        if (c >= 1 && issued < nchunks) {
+            bulk_wait_read_1();  // the previous piece's store has read its stage
+            issue(issued++);
+        }
+    }
+    if (!ok) {
+        atomicExch(flag, 1);
+        for (long long j = c; j < issued; ++j) {
+            const unsigned long long k = seq + (unsigned long long)j;
+            mbar_wait(&bar[k % kBulkStages], unsigned((k / kBulkStages) & 1));
+        }
+    }
+    bulk_wait_read_0();  // stages free for the next tile
+    seq += (unsigned long long)issued;
+    for (long long b = body; b < nbytes; ++b) d[b] = s[b];
+    return ok;
 }
 
 // Row-form gather / scatter over outputs (gather) or inputs (scatter)
@@ -145,8 +207,16 @@ __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, 
 template <int MINB>
 __global__ void __launch_bounds__(kBatchBlock, MINB)
 batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* __restrict__ tile_prefix,
-             unsigned long long* counter) {
+             unsigned long long* counter, int* flag) {
     __shared__ long long s_tile;
+    __shared__ __align__(8) unsigned long long s_bar[kBulkStages];
+    extern __shared__ __align__(128) unsigned char s_stage[];
+    unsigned long long seq = 0;  // thread 0: bulk loads issued so far
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kBulkStages; ++k) mbar_init(&s_bar[k], 1);
+        fence_mbarrier_init();
+    }
+    __syncthreads();
     const long long total = tile_prefix[ntasks];
     for (;;) {
         if (threadIdx.x == 0) s_tile = (long long)atomicAdd(counter, 1ull);
@@ -166,9 +236,18 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
         const long long first = (tile - __ldg(tile_prefix + lo)) * t.tile_structs;
         const long long cnt = t.n - first < t.tile_structs ? t.n - first : t.tile_structs;
         const long long w = 4ll * t.words;
-        if (t.op == TRV_OP_COPY)
-            tile_copy_flat(t.src + first * w, t.dst + first * w, cnt * w);
-        else if (t.op == TRV_OP_GATHER)
+        if (t.op == TRV_OP_COPY) {
+            const unsigned char* cs = t.src + first * w;
+            unsigned char* cd = t.dst + first * w;
+            const bool bulk = t.copy_bulk != 0 &&
+                              ((reinterpret_cast<uintptr_t>(cs) | reinterpret_cast<uintptr_t>(cd)) & 15u) == 0 &&
+                              cnt * w >= 16;
+            if (bulk) {
+                if (threadIdx.x == 0) tile_copy_bulk(cs, cd, cnt * w, s_stage, s_bar, seq, flag);
+            } else {
+                tile_copy_flat(cs, cd, cnt * w);
+            }
+        } else if (t.op == TRV_OP_GATHER)
             tile_index<true>(t, first, cnt);
         else
             tile_index<false>(t, first, cnt);
@@ -183,12 +262,17 @@ const void* batch_kernel_func(int blocks_per_sm) {
 
 cudaError_t launch_batch_kernel(const BatchTask* tasks, int ntasks, const long long* tile_prefix,
                                 unsigned long long* counter, int grid, int blocks_per_sm, cudaStream_t st) {
+    int* flag = device_flag();
+    if (!flag) return cudaErrorMemoryAllocation;
+    static_assert(kBulkSmem <= 48 * 1024, "stages fit the default dynamic shared memory limit");
     if (blocks_per_sm == 2)
-        batch_kernel<2><<<grid, kBatchBlock, 0, st>>>(tasks, ntasks, tile_prefix, counter);
+        batch_kernel<2><<<grid, kBatchBlock, kBulkSmem, st>>>(tasks, ntasks, tile_prefix, counter, flag);
     else
-        batch_kernel<4><<<grid, kBatchBlock, 0, st>>>(tasks, ntasks, tile_prefix, counter);
+        batch_kernel<4><<<grid, kBatchBlock, kBulkSmem, st>>>(tasks, ntasks, tile_prefix, counter, flag);
     return cudaGetLastError();
 }
+
+int batch_dynamic_smem() { return kBulkSmem; }
 
 int batch_block_threads() { return kBatchBlock; }
 

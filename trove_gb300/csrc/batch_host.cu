@@ -128,12 +128,15 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
                        : (tuned && c.cache_policy) ? c.cache_policy
                                                    : 1;
         d.l2_hint = (t.op == TRV_OP_GATHER && gp == 4) ? 1 : 0;
+        const int cp = (opt && opt->copy_path) ? opt->copy_path : (tuned && c.path) ? c.path : TRV_PATH_AUTO;
+        d.copy_bulk = cp == TRV_PATH_VECTOR ? 0 : 1;
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
         const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
         bytes += tb;
         if (tuned && c.grid == 2) vote2 += tb;
         if (tuned && c.grid == 4) vote4 += tb;
     }
+    if (!device_flag()) return TRV_ERR_CUDA;  // resolved now, outside any later graph capture
     trv_batch* b = new (std::nothrow) trv_batch;
     if (!b) return TRV_ERR_OUT_OF_MEMORY;
     cudaGetDevice(&b->device);

@@ -22,60 +22,12 @@
 #include <stdint.h>
 
 #include "bulk.h"
+#include "tma.cuh"
 
 namespace trv {
 namespace {
 
 constexpr int kStages = 4;
-constexpr unsigned kSpinLimit = 1u << 24;
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// true once the phase with the given parity has completed; false after
-// `polls` unsuccessful polls.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned polls = kSpinLimit) {
-    for (unsigned i = 0; i < polls; ++i) {
-        unsigned done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(smem_addr(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void bulk_load(void* smem, const void* gmem, unsigned bytes, unsigned long long* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(smem)),
-        "l"(gmem), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void bulk_store(void* gmem, const void* smem, unsigned bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gmem), "r"(smem_addr(smem)),
-                 "r"(bytes)
-                 : "memory");
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-
-__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 __global__ void __launch_bounds__(32)
 bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, long long nbytes, int head,
@@ -98,7 +50,7 @@ bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restric
     if (mine == 0) return;
 
     for (int k = 0; k < kStages; ++k) mbar_init(&bar[k], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_mbarrier_init();
 
     auto chunk_bytes = [&](long long c) -> unsigned {
         const long long off = c * chunk;
@@ -124,7 +76,7 @@ bulk_copy_kernel(const unsigned char* __restrict__ src, unsigned char* __restric
             ok = false;
             break;
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fence_proxy_async_shared();
         const long long c = blockIdx.x + k * (long long)gridDim.x;
         bulk_store(d + c * chunk, stage_mem + (size_t)st * chunk, chunk_bytes(c));
         if (k >= 1 && issued < mine) {

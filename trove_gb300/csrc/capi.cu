@@ -51,22 +51,23 @@ DeviceInfo& device_info() {
     return d;
 }
 
+// The error flag is a module-scope device variable (one per device, zero at
+// load), so finding it allocates nothing: callers that must not allocate
+// (trv_batch_run_static) and stream capture can use it.  Resolve it outside
+// a capture the first time (trv_batch_create and trv_server_create do).
+__device__ int g_device_flag;
+
 int* device_flag() {
     static std::mutex mu;
     DeviceInfo& d = device_info();
     std::lock_guard<std::mutex> g(mu);
     if (!d.flag) {
-        int* p = nullptr;
-        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_flag) != cudaSuccess) {
             cudaGetLastError();
             return nullptr;
         }
-        if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) {
-            cudaGetLastError();
-            cudaFree(p);
-            return nullptr;
-        }
-        d.flag = p;
+        d.flag = static_cast<int*>(p);
     }
     return d.flag;
 }

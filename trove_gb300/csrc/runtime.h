@@ -18,8 +18,8 @@ struct DeviceInfo {
 // Properties of the calling thread's current device (cached).
 DeviceInfo& device_info();
 
-// The current device's error flag (allocated and zeroed on first use), or
-// nullptr if that allocation failed.
+// The current device's error flag (a device variable found on first use),
+// or nullptr if it cannot be found.
 int* device_flag();
 
 // Resident blocks of `func` at `block` threads across the whole GPU.

@@ -225,6 +225,7 @@ struct trv_server {
                               : (r.r.width % 8 == 0 && (al & 7u) == 0) ? 3
                                                                         : 2;
                 d.l2_hint = 0;
+                d.copy_bulk = 1;
                 s.h_prefix[k] = tiles;
                 tiles += (d.n + tile - 1) / tile;
                 r.phase = LAUNCHED;
@@ -321,6 +322,7 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
     *out = nullptr;
     if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_batch_requests < 0 || cfg->tile_bytes < 0)
         return TRV_ERR_INVALID_ARGUMENT;
+    if (!device_flag()) return TRV_ERR_CUDA;  // the batch kernel's error flag, found before the dispatcher runs
     trv_server* s = new (std::nothrow) trv_server;
     if (!s) return TRV_ERR_OUT_OF_MEMORY;
     s->cfg = *cfg;
