@@ -236,12 +236,15 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         const int op = std::get<0>(kv.first);
         // (tile_bytes, blocks per SM, gather load policy, copy tile path)
         std::vector<std::tuple<int, int, int, int>> cands;
-        for (int tb : {16 << 10, 64 << 10, 256 << 10, 1 << 20})
+        for (int tb : {64 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
                 for (int gp : {1, 4})
                     for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
                         if (gp == 4 && op != TRV_OP_GATHER) continue;
                         if (cpath == TRV_PATH_VECTOR && op != TRV_OP_COPY) continue;
+                        // the register budget is one per batch and set by its
+                        // gathers and scatters; copy tiles hardly use registers
+                        if (bps == 4 && op == TRV_OP_COPY) continue;
                         cands.push_back({tb, bps, gp, cpath});
                     }
         float best = -1.f;

@@ -97,7 +97,9 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
     uint64_t bytes = 0;
-    uint64_t vote2 = 0, vote4 = 0;  // bytes of tasks whose tuned entry prefers 2 / 4 blocks per SM
+    // bytes of gather / scatter tasks whose tuned entry prefers 2 / 4 blocks per
+    // SM (their movers set the register budget; copy tiles barely use one)
+    uint64_t vote2 = 0, vote4 = 0;
     for (uint64_t k = 0; k < count; ++k) {
         const trv_task& t = tasks[k];
         const int rc = validate(t);
@@ -133,8 +135,8 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
         const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
         bytes += tb;
-        if (tuned && c.grid == 2) vote2 += tb;
-        if (tuned && c.grid == 4) vote4 += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 2) vote2 += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 4) vote4 += tb;
     }
     if (!device_flag()) return TRV_ERR_CUDA;  // resolved now, outside any later graph capture
     trv_batch* b = new (std::nothrow) trv_batch;

@@ -97,8 +97,8 @@ int plan_static(const trv_task* tasks, uint64_t count, const trv_batch_options* 
         d.copy_bulk = opt && opt->copy_path == TRV_PATH_VECTOR ? 0 : 1;
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
         const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
-        if (tuned && c.grid == 2) vote2 += tb;
-        if (tuned && c.grid == 4) vote4 += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 2) vote2 += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 4) vote4 += tb;
     }
     *blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote4 > vote2 ? 4 : 2);
     return TRV_OK;
