@@ -224,8 +224,9 @@ typedef struct trv_batch_options {
     int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
     int32_t blocks_per_sm; /* 2: 128 registers per thread (0: the autotuned or default choice, 2);
                               4: 64 registers, twice the warps */
-    int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (1);
-                              1 plain; 4 with the 64-byte L2 prefetch-size hint */
+    int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (5);
+                              1 plain; 4 with the 64-byte L2 prefetch-size hint; 5 rows staged
+                              through shared memory with asynchronous copies (cp.async) */
 } trv_batch_options;
 
 typedef struct trv_batch trv_batch;

@@ -120,7 +120,7 @@ def check(tasks, expect):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gather_policy", [0, 1, 4])
+@pytest.mark.parametrize("gather_policy", [0, 1, 4, 5])
 @pytest.mark.parametrize("copy_path", ["vector", "auto"])
 @pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
 def test_batch_matches_oracle(cuda, copy_path, tile_bytes, gather_policy):

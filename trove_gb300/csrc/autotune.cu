@@ -238,9 +238,9 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         std::vector<std::tuple<int, int, int, int>> cands;
         for (int tb : {64 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
-                for (int gp : {1, 4})
+                for (int gp : {1, 4, 5})
                     for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
-                        if (gp == 4 && op != TRV_OP_GATHER) continue;
+                        if (gp != 1 && op != TRV_OP_GATHER) continue;
                         if (cpath == TRV_PATH_VECTOR && op != TRV_OP_COPY) continue;
                         // the register budget is one per batch and set by its
                         // gathers and scatters; copy tiles hardly use registers

@@ -39,6 +39,7 @@ constexpr int kWarps = kBatchBlock / 32;
 constexpr int kBulkStages = 4;
 constexpr int kBulkChunk = 8 << 10;
 constexpr int kBulkSmem = kBulkStages * kBulkChunk;
+constexpr int kIdxSlots = 1024;  // indices per piece of a staged gather (two pieces' worth in shared memory)
 
 // ---- per-tile movers (all warps of the CTA cooperate on one tile) --------
 
@@ -100,6 +101,7 @@ __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long lo
         bulk_load(stage + (size_t)st * kBulkChunk, s + c * kBulkChunk, chunk_bytes(c), &bar[st]);
     };
     const long long prologue = nchunks < kBulkStages ? nchunks : kBulkStages;
+    fence_proxy_async_shared();  // earlier generic-proxy use of the stages (gather tiles) before TMA writes
     for (long long c = 0; c < prologue; ++c) issue(c);
     long long issued = prologue;
     bool ok = true;
@@ -186,6 +188,78 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
     }
 }
 
+// Gather of outputs [first, first + cnt) staged through shared memory with
+// cp.async: the warps issue asynchronous word copies from the random source
+// rows straight into a shared-memory buffer (no registers hold the data in
+// flight, so far more of it can be), then write the buffer out to the
+// contiguous destination with coalesced stores.  Two buffers of kBulkSmem / 2
+// bytes alternate, so the next piece's copies are in flight while the
+// current one is written.  Word q of a piece (words of sizeof(V)) belongs to
+// struct q / m; its index is read through the read-only cache.
+__device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int bytes) {
+    const unsigned s = smem_addr(smem);
+    if (bytes == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+    else if (bytes == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+template <typename V>
+__device__ void tile_gather_async(const V* src, V* dst, const int* idx, long long bound, long long first,
+                                  long long cnt, int m, unsigned char* stage, int* s_idx) {
+    const int tid = opaque_tid();
+    constexpr int kPieceBytes = kBulkSmem / 2;
+    // structs per piece: a multiple of 32 that fits the buffer and the index slots
+    int per = (kPieceBytes / int(sizeof(V))) / m / 32 * 32;
+    if (per > kIdxSlots) per = kIdxSlots;
+    // q / m for q < 2^12 and m <= 16 as a multiply and shift (exact there)
+    const unsigned inv_m = (65536u + unsigned(m) - 1) / unsigned(m);
+    const long long pieces = (cnt + per - 1) / per;
+    auto issue = [&](long long p) {
+        V* buf = reinterpret_cast<V*>(stage + (p & 1) * kPieceBytes);
+        int* ix = s_idx + (p & 1) * kIdxSlots;
+        const long long base = first + p * per;
+        const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
+        for (int j = tid; j < n_here; j += kBatchBlock) {
+            const int v = __ldcs(idx + base + j);
+            ix[j] = (v >= 0 && (long long)v < bound) ? v : -1;
+        }
+        __syncthreads();
+        const int words = n_here * m;
+        for (int q = tid; q < words; q += kBatchBlock) {
+            const int j = int((unsigned(q) * inv_m) >> 16);
+            const int v = ix[j];
+            if (v >= 0) cp_async_word(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    auto drain = [&](long long p) {
+        const V* buf = reinterpret_cast<const V*>(stage + (p & 1) * kPieceBytes);
+        const int* ix = s_idx + (p & 1) * kIdxSlots;
+        const long long base = first + p * per;
+        const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
+        const int words = n_here * m;
+        for (int q = tid; q < words; q += kBatchBlock) {
+            const int j = int((unsigned(q) * inv_m) >> 16);
+            if (ix[j] >= 0) __stcs(dst + base * m + q, buf[q]);
+        }
+    };
+    issue(0);
+    for (long long p = 0; p < pieces; ++p) {
+        if (p + 1 < pieces) {
+            issue(p + 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        drain(p);
+        __syncthreads();  // buffer and index slots are refilled by issue(p + 2)
+    }
+}
+
 template <bool GATHER>
 __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, long long cnt) {
     const int m = t.words * 4 >> t.word_log2;
@@ -210,6 +284,7 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
              unsigned long long* counter, int* flag) {
     __shared__ long long s_tile;
     __shared__ __align__(8) unsigned long long s_bar[kBulkStages];
+    __shared__ int s_idx[2 * kIdxSlots];
     extern __shared__ __align__(128) unsigned char s_stage[];
     unsigned long long seq = 0;  // thread 0: bulk loads issued so far
     if (threadIdx.x == 0) {
@@ -247,8 +322,22 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
             } else {
                 tile_copy_flat(cs, cd, cnt * w);
             }
-        } else if (t.op == TRV_OP_GATHER)
-            tile_index<true>(t, first, cnt);
+        } else if (t.op == TRV_OP_GATHER) {
+            if (t.l2_hint == 2) {  // staged through shared memory
+                const int m = t.words * 4 >> t.word_log2;
+                if (t.word_log2 == 4)
+                    tile_gather_async(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst), t.idx,
+                                      t.bound, first, cnt, m, s_stage, s_idx);
+                else if (t.word_log2 == 3)
+                    tile_gather_async(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst), t.idx,
+                                      t.bound, first, cnt, m, s_stage, s_idx);
+                else
+                    tile_gather_async(reinterpret_cast<const unsigned*>(t.src), reinterpret_cast<unsigned*>(t.dst),
+                                      t.idx, t.bound, first, cnt, m, s_stage, s_idx);
+            } else {
+                tile_index<true>(t, first, cnt);
+            }
+        }
         else
             tile_index<false>(t, first, cnt);
     }

@@ -16,7 +16,8 @@ struct alignas(16) BatchTask {
     int words;        // struct width / 4
     int tile_structs; // structs per tile, a multiple of 32
     int word_log2;    // gather / scatter: log2 of the word moved per lane (2, 3 or 4)
-    int l2_hint;      // gather: 1 = random loads carry the 64-byte L2 prefetch-size hint
+    int l2_hint;      // gather: 1 = random loads carry the 64-byte L2 prefetch-size hint,
+                      // 2 = rows staged through shared memory with cp.async
     int copy_bulk;    // copy: 1 = TMA bulk tiles where 16-byte aligned, 0 = flat vector tiles
 };
 

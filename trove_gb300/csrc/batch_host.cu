@@ -92,7 +92,8 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     if (opt && opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
     if (opt && opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4)
         return TRV_ERR_UNSUPPORTED;
-    if (opt && opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4)
+    if (opt && opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4 &&
+        opt->gather_policy != 5)
         return TRV_ERR_INVALID_ARGUMENT;
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
@@ -123,13 +124,14 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         d.words = int(t.width / 4);
         d.tile_structs = int(tile);
         d.word_log2 = batch_word_log2(t);
-        // Gather loads: plain unless chosen otherwise.  The hint measured 3 %
-        // slower on the 4096-array workload's uniform-index gathers, most of
-        // whose sources are small enough to be L2-resident.
+        // Gather rows are staged through shared memory with cp.async unless
+        // chosen otherwise: on the 4096-array workload its gathers ran 25 %
+        // faster that way (14.9 vs 18.7 ms) than with register-held rows,
+        // whose 128-register kernel keeps only 2 blocks per SM resident.
         const int gp = (opt && opt->gather_policy) ? opt->gather_policy
                        : (tuned && c.cache_policy) ? c.cache_policy
-                                                   : 1;
-        d.l2_hint = (t.op == TRV_OP_GATHER && gp == 4) ? 1 : 0;
+                                                   : 5;
+        d.l2_hint = t.op != TRV_OP_GATHER ? 0 : gp == 4 ? 1 : gp == 5 ? 2 : 0;
         const int cp = (opt && opt->copy_path) ? opt->copy_path : (tuned && c.path) ? c.path : TRV_PATH_AUTO;
         d.copy_bulk = cp == TRV_PATH_VECTOR ? 0 : 1;
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;

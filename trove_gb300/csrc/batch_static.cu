@@ -93,7 +93,8 @@ int plan_static(const trv_task* tasks, uint64_t count, const trv_batch_options* 
         d.words = int(t.width / 4);
         d.tile_structs = int(tile);
         d.word_log2 = (t.width % 16 == 0 && (al & 15u) == 0) ? 4 : (t.width % 8 == 0 && (al & 7u) == 0) ? 3 : 2;
-        d.l2_hint = t.op == TRV_OP_GATHER && opt && opt->gather_policy == 4 ? 1 : 0;
+        const int gp = (opt && opt->gather_policy) ? opt->gather_policy : 5;
+        d.l2_hint = t.op != TRV_OP_GATHER ? 0 : gp == 4 ? 1 : gp == 5 ? 2 : 0;
         d.copy_bulk = opt && opt->copy_path == TRV_PATH_VECTOR ? 0 : 1;
         prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
         const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);

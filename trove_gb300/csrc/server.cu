@@ -224,7 +224,7 @@ struct trv_server {
                 d.word_log2 = (r.r.width % 16 == 0 && (al & 15u) == 0) ? 4
                               : (r.r.width % 8 == 0 && (al & 7u) == 0) ? 3
                                                                         : 2;
-                d.l2_hint = 0;
+                d.l2_hint = r.r.op == TRV_OP_GATHER ? 2 : 0;  // rows staged through shared memory
                 d.copy_bulk = 1;
                 s.h_prefix[k] = tiles;
                 tiles += (d.n + tile - 1) / tile;
