@@ -222,11 +222,15 @@ typedef struct trv_batch_options {
                             where source and destination are 16-byte aligned) or
                             TRV_PATH_VECTOR (flat vector tiles) */
     int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
-    int32_t blocks_per_sm; /* 2: 128 registers per thread (0: the autotuned or default choice, 2);
-                              4: 64 registers, twice the warps */
+    int32_t blocks_per_sm; /* resident blocks per SM: 4 (64 registers per thread) or 2 (128, for
+                              the register-held gather / scatter rows of policy 1 and 4);
+                              0: the autotuned or default choice (4) */
     int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (5);
                               1 plain; 4 with the 64-byte L2 prefetch-size hint; 5 rows staged
                               through shared memory with asynchronous copies (cp.async) */
+    int32_t scatter_policy; /* scatter tasks: 0 the autotuned or default choice (5); 1 rows held
+                               in registers; 5 the contiguous source staged through shared
+                               memory with cp.async, stored to the random rows from there */
 } trv_batch_options;
 
 typedef struct trv_batch trv_batch;

@@ -62,9 +62,10 @@ def test_batch_argument_errors(trove_lib):
     for bad_path in ["bulk", "warp"]:
         with pytest.raises(tg.TroveError):
             tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path=bad_path)
-    with pytest.raises(tg.TroveError) as e:
-        tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], gather_policy=2)
-    assert e.value.status == 1
+    for bad in (dict(gather_policy=2), dict(scatter_policy=4), dict(scatter_policy=-1)):
+        with pytest.raises(tg.TroveError) as e:
+            tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], **bad)
+        assert e.value.status == 1
 
 
 def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000):
@@ -99,9 +100,17 @@ def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000)
             e = e.reshape(-1)
         else:
             idx_h = oracle.permutation(n, seed + k) if n else np.zeros(1, np.int32)
-            idx_t = torch.from_numpy(idx_h.copy()).cuda()
             bound = n
-            e = oracle.scatter(init, src_h, idx_h, n, w) if n else init.copy()
+            if n > 10:  # skipped: the destination keeps its sentinel at those rows
+                idx_h[5] = -1
+                idx_h[9] = n + 3
+                ok = (idx_h[:n] >= 0) & (idx_h[:n] < n)
+                e = init.copy().reshape(-1, w)
+                e[idx_h[:n][ok]] = src_h[ok]
+                e = e.reshape(-1)
+            else:
+                e = oracle.scatter(init, src_h, idx_h, n, w) if n else init.copy()
+            idx_t = torch.from_numpy(idx_h.copy()).cuda()
         tasks.append(dict(op=op, width=w, n=n, src=src, dst=dst, idx=idx_t, bound=bound))
         expect.append(e)
         outs.append(dst)
@@ -120,13 +129,14 @@ def check(tasks, expect):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gather_policy", [0, 1, 4, 5])
+@pytest.mark.parametrize("gather_policy,scatter_policy", [(0, 0), (1, 1), (4, 5), (5, 1), (1, 5)])
 @pytest.mark.parametrize("copy_path", ["vector", "auto"])
 @pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
-def test_batch_matches_oracle(cuda, copy_path, tile_bytes, gather_policy):
+def test_batch_matches_oracle(cuda, copy_path, tile_bytes, gather_policy, scatter_policy):
     torch = cuda
     tasks, expect = make_workload(torch, 120, seed=3)
-    b = tg.Batch(tasks, tile_bytes=tile_bytes, copy_path=copy_path, gather_policy=gather_policy)
+    b = tg.Batch(tasks, tile_bytes=tile_bytes, copy_path=copy_path, gather_policy=gather_policy,
+                 scatter_policy=scatter_policy)
     tiles, nbytes = b.info()
     assert tiles > 0 and nbytes > 0
     b.launch()
@@ -153,6 +163,24 @@ def test_batch_graph_replay_and_per_call(cuda):
     torch.cuda.synchronize()
     check(tasks, expect)
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("blocks_per_sm", [2, 4])
+@pytest.mark.parametrize("policy", [1, 5])
+def test_batch_register_budgets(cuda, blocks_per_sm, policy):
+    """Both kernel builds (2 and 4 resident blocks per SM) with register-held
+    and shared-memory-staged gather / scatter rows, at several tile sizes."""
+    torch = cuda
+    tasks, expect = make_workload(torch, 80, seed=21, widths=tuple(range(4, 65, 4)))
+    for tile_bytes in (0, 2048, 1 << 18):
+        reset(tasks)
+        b = tg.Batch(tasks, tile_bytes=tile_bytes, blocks_per_sm=blocks_per_sm, gather_policy=policy,
+                     scatter_policy=policy)
+        b.launch()
+        torch.cuda.synchronize()
+        check(tasks, expect)
+        b.close()
 
 
 @pytest.mark.gpu

@@ -73,7 +73,8 @@ class Task(ctypes.Structure):
 
 class BatchOptions(ctypes.Structure):
     _fields_ = [("tile_bytes", ctypes.c_int32), ("copy_path", ctypes.c_int32), ("grid_blocks", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32), ("gather_policy", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("gather_policy", ctypes.c_int32),
+                ("scatter_policy", ctypes.c_int32)]
 
 
 _lib = None
@@ -314,11 +315,12 @@ class Batch:
     persistent kernel; capture() records it as a CUDA graph first."""
 
     def __init__(self, tasks, *, tile_bytes: int = 0, copy_path=PATH_AUTO, grid: int = 0, blocks_per_sm: int = 0,
-                 gather_policy: int = 0):
+                 gather_policy: int = 0, scatter_policy: int = 0):
         if isinstance(copy_path, str):
             copy_path = PATHS[copy_path]
         self._tasks = make_tasks(tasks)
-        opt = BatchOptions(int(tile_bytes), int(copy_path), int(grid), int(blocks_per_sm), int(gather_policy))
+        opt = BatchOptions(int(tile_bytes), int(copy_path), int(grid), int(blocks_per_sm), int(gather_policy),
+                           int(scatter_policy))
         h = ctypes.c_void_p()
         _check(load().trv_batch_create(self._tasks, len(self._tasks), ctypes.byref(opt), ctypes.byref(h)),
                "trv_batch_create")

@@ -234,24 +234,28 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         groups[std::make_tuple(tasks[k].op, int(tasks[k].width), len_bucket(tasks[k].n))].push_back(tasks[k]);
     for (auto& kv : groups) {
         const int op = std::get<0>(kv.first);
-        // (tile_bytes, blocks per SM, gather load policy, copy tile path)
+        // (tile_bytes, blocks per SM, gather / scatter policy, copy tile path)
         std::vector<std::tuple<int, int, int, int>> cands;
         for (int tb : {64 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
                 for (int gp : {1, 4, 5})
                     for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
-                        if (gp != 1 && op != TRV_OP_GATHER) continue;
+                        if (gp == 4 && op != TRV_OP_GATHER) continue;  // a load hint
+                        if (gp != 1 && op == TRV_OP_COPY) continue;
                         if (cpath == TRV_PATH_VECTOR && op != TRV_OP_COPY) continue;
                         // the register budget is one per batch and set by its
-                        // gathers and scatters; copy tiles hardly use registers
-                        if (bps == 4 && op == TRV_OP_COPY) continue;
+                        // gathers and scatters; copy groups are timed at the
+                        // default budget (4 blocks per SM)
+                        if (bps == 2 && op == TRV_OP_COPY) continue;
                         cands.push_back({tb, bps, gp, cpath});
                     }
         float best = -1.f;
         std::tuple<int, int, int, int> pick{0, 0, 0, 0};
         uint64_t bytes = 0;
         for (const auto& c : cands) {
-            trv_batch_options o{std::get<0>(c), std::get<3>(c), 0, std::get<1>(c), std::get<2>(c)};
+            const int gp = std::get<2>(c);
+            trv_batch_options o{std::get<0>(c), std::get<3>(c), 0, std::get<1>(c), op == TRV_OP_GATHER ? gp : 0,
+                                op == TRV_OP_SCATTER ? gp : 0};
             trv_batch* b = nullptr;
             int rc = trv_batch_create(kv.second.data(), kv.second.size(), &o, &b);
             if (rc != TRV_OK) return rc;

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -39,7 +40,18 @@ constexpr int kWarps = kBatchBlock / 32;
 constexpr int kBulkStages = 4;
 constexpr int kBulkChunk = 8 << 10;
 constexpr int kBulkSmem = kBulkStages * kBulkChunk;
-constexpr int kIdxSlots = 1024;  // indices per piece of a staged gather (two pieces' worth in shared memory)
+// Staged gathers and scatters (below) cycle through kStagedPieces buffers of
+// kPieceBytes, each with kIdxSlots index slots.  Two pieces per block: four
+// per block measured slower (18.5 vs 14.9 ms for the 4096-array batch's
+// gathers at 2 blocks per SM); more resident blocks is what pays (11.7 ms at
+// 4 blocks per SM), as block barriers then overlap.  The copy ring reuses the
+// first kBulkSmem bytes of the same buffer.
+constexpr int kPieceBytes = 16 << 10;
+constexpr int kIdxSlots = 1024;
+constexpr int kStagedPieces = 2;
+template <int MINB>
+constexpr int kDynSmem = kStagedPieces * (kPieceBytes + kIdxSlots * int(sizeof(int)));
+static_assert(kBulkSmem <= kStagedPieces * kPieceBytes, "the copy ring fits the piece buffers");
 
 // ---- per-tile movers (all warps of the CTA cooperate on one tile) --------
 
@@ -188,14 +200,18 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
     }
 }
 
-// Gather of outputs [first, first + cnt) staged through shared memory with
-// cp.async: the warps issue asynchronous word copies from the random source
-// rows straight into a shared-memory buffer (no registers hold the data in
-// flight, so far more of it can be), then write the buffer out to the
-// contiguous destination with coalesced stores.  Two buffers of kBulkSmem / 2
-// bytes alternate, so the next piece's copies are in flight while the
-// current one is written.  Word q of a piece (words of sizeof(V)) belongs to
-// struct q / m; its index is read through the read-only cache.
+// Gather / scatter of the structs [first, first + cnt) of the contiguous side
+// staged through shared memory with cp.async.  Gather: the warps issue
+// asynchronous word copies from the random source rows straight into a
+// shared-memory buffer (no registers hold the data in flight, so far more of
+// it can be), then write the buffer out to the contiguous destination with
+// coalesced stores.  Scatter: the contiguous source piece is copied in the
+// same way, then each word is stored to its random destination row from
+// shared memory (stores need no registers held in flight either).  D buffers
+// of kPieceBytes rotate, so the copies of the next D - 1 pieces are in flight
+// while the current one is written.  Word q of a piece (words of sizeof(V))
+// belongs to struct q / m; the piece's indices are staged in shared memory
+// first (one coalesced read), invalid ones marked -1.
 __device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int bytes) {
     const unsigned s = smem_addr(smem);
     if (bytes == 16)
@@ -206,11 +222,23 @@ __device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int 
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
 }
 
-template <typename V>
-__device__ void tile_gather_async(const V* src, V* dst, const int* idx, long long bound, long long first,
+// Waits until at most n of this thread's cp.async groups are pending.
+__device__ __forceinline__ void cp_async_wait_pending(int n) {
+    if (n <= 0)
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+    else if (n == 1)
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else if (n == 2)
+        asm volatile("cp.async.wait_group 2;" ::: "memory");
+    else
+        asm volatile("cp.async.wait_group 3;" ::: "memory");
+}
+
+template <typename V, int D, bool GATHER>
+__device__ void tile_index_staged(const V* src, V* dst, const int* idx, long long bound, long long first,
                                   long long cnt, int m, unsigned char* stage, int* s_idx) {
+    static_assert(D >= 2 && D <= 4, "wait depths 0..3");
     const int tid = opaque_tid();
-    constexpr int kPieceBytes = kBulkSmem / 2;
     // structs per piece: a multiple of 32 that fits the buffer and the index slots
     int per = (kPieceBytes / int(sizeof(V))) / m / 32 * 32;
     if (per > kIdxSlots) per = kIdxSlots;
@@ -218,45 +246,55 @@ __device__ void tile_gather_async(const V* src, V* dst, const int* idx, long lon
     const unsigned inv_m = (65536u + unsigned(m) - 1) / unsigned(m);
     const long long pieces = (cnt + per - 1) / per;
     auto issue = [&](long long p) {
-        V* buf = reinterpret_cast<V*>(stage + (p & 1) * kPieceBytes);
-        int* ix = s_idx + (p & 1) * kIdxSlots;
+        const int b = int(p % D);
+        V* buf = reinterpret_cast<V*>(stage + b * kPieceBytes);
+        int* ix = s_idx + b * kIdxSlots;
         const long long base = first + p * per;
         const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
         for (int j = tid; j < n_here; j += kBatchBlock) {
             const int v = __ldcs(idx + base + j);
             ix[j] = (v >= 0 && (long long)v < bound) ? v : -1;
         }
-        __syncthreads();
         const int words = n_here * m;
-        for (int q = tid; q < words; q += kBatchBlock) {
-            const int j = int((unsigned(q) * inv_m) >> 16);
-            const int v = ix[j];
-            if (v >= 0) cp_async_word(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
+        if (GATHER) {
+            __syncthreads();  // the copies below read the staged indices
+            for (int q = tid; q < words; q += kBatchBlock) {
+                const int j = int((unsigned(q) * inv_m) >> 16);
+                const int v = ix[j];
+                if (v >= 0) cp_async_word(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
+            }
+        } else {  // indices are next read after the wait's barrier
+            for (int q = tid; q < words; q += kBatchBlock) cp_async_word(buf + q, src + base * m + q, int(sizeof(V)));
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     auto drain = [&](long long p) {
-        const V* buf = reinterpret_cast<const V*>(stage + (p & 1) * kPieceBytes);
-        const int* ix = s_idx + (p & 1) * kIdxSlots;
+        const int b = int(p % D);
+        const V* buf = reinterpret_cast<const V*>(stage + b * kPieceBytes);
+        const int* ix = s_idx + b * kIdxSlots;
         const long long base = first + p * per;
         const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
         const int words = n_here * m;
         for (int q = tid; q < words; q += kBatchBlock) {
             const int j = int((unsigned(q) * inv_m) >> 16);
-            if (ix[j] >= 0) __stcs(dst + base * m + q, buf[q]);
+            const int v = ix[j];
+            if (v < 0) continue;
+            if (GATHER)
+                __stcs(dst + base * m + q, buf[q]);
+            else
+                dst[(long long)v * m + (q - j * m)] = buf[q];
         }
     };
-    issue(0);
+    for (long long p = 0; p < D - 1 && p < pieces; ++p) issue(p);
     for (long long p = 0; p < pieces; ++p) {
-        if (p + 1 < pieces) {
-            issue(p + 1);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
+        // buffer (p + D - 1) % D was drained in the previous iteration
+        if (p + D - 1 < pieces) issue(p + D - 1);
+        // groups committed: min(p + D, pieces); piece p's must be complete
+        const long long later = pieces - 1 - p;
+        cp_async_wait_pending(later < D - 1 ? int(later) : D - 1);
         __syncthreads();
         drain(p);
-        __syncthreads();  // buffer and index slots are refilled by issue(p + 2)
+        __syncthreads();  // buffer and index slots are refilled by issue(p + D)
     }
 }
 
@@ -265,14 +303,31 @@ __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, 
     const int m = t.words * 4 >> t.word_log2;
     if (t.word_log2 == 4)
         tile_index_rows<uint4, 2, 2, GATHER>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
-                                             t.idx, t.bound, first, cnt, m, t.l2_hint != 0);
+                                             t.idx, t.bound, first, cnt, m, t.index_mode == 1);
     else if (t.word_log2 == 3)
         tile_index_rows<uint2, 2, 4, GATHER>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
-                                             t.idx, t.bound, first, cnt, m, t.l2_hint != 0);
+                                             t.idx, t.bound, first, cnt, m, t.index_mode == 1);
     else
         tile_index_rows<unsigned, 2, 4, GATHER>(reinterpret_cast<const unsigned*>(t.src),
                                                 reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m,
-                                                t.l2_hint != 0);
+                                                t.index_mode == 1);
+}
+
+template <bool GATHER>
+__device__ __forceinline__ void tile_staged(const BatchTask& t, long long first, long long cnt, int m,
+                                            unsigned char* stage, int* s_idx) {
+    if (t.word_log2 == 4)
+        tile_index_staged<uint4, kStagedPieces, GATHER>(reinterpret_cast<const uint4*>(t.src),
+                                                        reinterpret_cast<uint4*>(t.dst), t.idx, t.bound, first, cnt,
+                                                        m, stage, s_idx);
+    else if (t.word_log2 == 3)
+        tile_index_staged<uint2, kStagedPieces, GATHER>(reinterpret_cast<const uint2*>(t.src),
+                                                        reinterpret_cast<uint2*>(t.dst), t.idx, t.bound, first, cnt,
+                                                        m, stage, s_idx);
+    else
+        tile_index_staged<unsigned, kStagedPieces, GATHER>(reinterpret_cast<const unsigned*>(t.src),
+                                                           reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first,
+                                                           cnt, m, stage, s_idx);
 }
 
 // MINB resident blocks per SM: 2 gives each thread 128 registers (no
@@ -284,8 +339,8 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
              unsigned long long* counter, int* flag) {
     __shared__ long long s_tile;
     __shared__ __align__(8) unsigned long long s_bar[kBulkStages];
-    __shared__ int s_idx[2 * kIdxSlots];
-    extern __shared__ __align__(128) unsigned char s_stage[];
+    extern __shared__ __align__(128) unsigned char s_stage[];  // kDynSmem<MINB> bytes
+    int* s_idx = reinterpret_cast<int*>(s_stage + kStagedPieces * kPieceBytes);
     unsigned long long seq = 0;  // thread 0: bulk loads issued so far
     if (threadIdx.x == 0) {
         for (int k = 0; k < kBulkStages; ++k) mbar_init(&s_bar[k], 1);
@@ -322,47 +377,59 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
             } else {
                 tile_copy_flat(cs, cd, cnt * w);
             }
+        } else if (t.index_mode == 2) {  // gather / scatter staged through shared memory
+            const int m = t.words * 4 >> t.word_log2;
+            if (t.op == TRV_OP_GATHER)
+                tile_staged<true>(t, first, cnt, m, s_stage, s_idx);
+            else
+                tile_staged<false>(t, first, cnt, m, s_stage, s_idx);
         } else if (t.op == TRV_OP_GATHER) {
-            if (t.l2_hint == 2) {  // staged through shared memory
-                const int m = t.words * 4 >> t.word_log2;
-                if (t.word_log2 == 4)
-                    tile_gather_async(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst), t.idx,
-                                      t.bound, first, cnt, m, s_stage, s_idx);
-                else if (t.word_log2 == 3)
-                    tile_gather_async(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst), t.idx,
-                                      t.bound, first, cnt, m, s_stage, s_idx);
-                else
-                    tile_gather_async(reinterpret_cast<const unsigned*>(t.src), reinterpret_cast<unsigned*>(t.dst),
-                                      t.idx, t.bound, first, cnt, m, s_stage, s_idx);
-            } else {
-                tile_index<true>(t, first, cnt);
-            }
-        }
-        else
+            tile_index<true>(t, first, cnt);
+        } else {
             tile_index<false>(t, first, cnt);
+        }
     }
 }
 
 }  // namespace
 
-const void* batch_kernel_func(int blocks_per_sm) {
-    return blocks_per_sm == 2 ? (const void*)&batch_kernel<2> : (const void*)&batch_kernel<4>;
+// Per device: the kernels' dynamic shared memory limit raised to their
+// staging buffers (once) and their resident blocks with that memory.
+int batch_grid(int blocks_per_sm) {
+    static std::mutex mu;
+    static int resident[64][2] = {};
+    DeviceInfo& d = device_info();
+    if (d.device < 0 || d.device >= 64) return 0;
+    const int which = blocks_per_sm == 2 ? 0 : 1;
+    std::lock_guard<std::mutex> g(mu);
+    if (!resident[d.device][0]) {
+        int r2 = 0, r4 = 0;
+        if (cudaFuncSetAttribute(batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem<2>) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(batch_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem<4>) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r2, batch_kernel<2>, kBatchBlock, kDynSmem<2>) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r4, batch_kernel<4>, kBatchBlock, kDynSmem<4>) !=
+                cudaSuccess || r2 < 1 || r4 < 1) {
+            cudaGetLastError();
+            return 0;
+        }
+        resident[d.device][0] = r2 * d.sm_count;
+        resident[d.device][1] = r4 * d.sm_count;
+    }
+    return resident[d.device][which];
 }
 
 cudaError_t launch_batch_kernel(const BatchTask* tasks, int ntasks, const long long* tile_prefix,
                                 unsigned long long* counter, int grid, int blocks_per_sm, cudaStream_t st) {
     int* flag = device_flag();
     if (!flag) return cudaErrorMemoryAllocation;
-    static_assert(kBulkSmem <= 48 * 1024, "stages fit the default dynamic shared memory limit");
     if (blocks_per_sm == 2)
-        batch_kernel<2><<<grid, kBatchBlock, kBulkSmem, st>>>(tasks, ntasks, tile_prefix, counter, flag);
+        batch_kernel<2><<<grid, kBatchBlock, kDynSmem<2>, st>>>(tasks, ntasks, tile_prefix, counter, flag);
     else
-        batch_kernel<4><<<grid, kBatchBlock, kBulkSmem, st>>>(tasks, ntasks, tile_prefix, counter, flag);
+        batch_kernel<4><<<grid, kBatchBlock, kDynSmem<4>, st>>>(tasks, ntasks, tile_prefix, counter, flag);
     return cudaGetLastError();
 }
-
-int batch_dynamic_smem() { return kBulkSmem; }
-
-int batch_block_threads() { return kBatchBlock; }
 
 }  // namespace trv

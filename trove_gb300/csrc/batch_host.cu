@@ -28,6 +28,30 @@ struct trv_batch {
 
 namespace {
 
+// A batch's plan lives on the device that was current when it was created.
+bool on_batch_device(const trv_batch* b) {
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && dev == b->device;
+}
+
+void release(trv_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_tasks) cudaFree(b->d_tasks);
+    if (b->d_prefix) cudaFree(b->d_prefix);
+    if (b->d_counter) cudaFree(b->d_counter);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->d_tasks = nullptr;
+    b->d_prefix = nullptr;
+    b->d_counter = nullptr;
+}
+
+}  // namespace
+
+namespace trv {
+namespace {
+
 bool aligned4(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; }
 
 int validate(const trv_task& t) {
@@ -45,39 +69,93 @@ int validate(const trv_task& t) {
     return TRV_OK;
 }
 
-// Word moved per lane by the row-form index movers: the widest of 16 / 8 / 4
-// bytes that divides the width and that both arrays are aligned to.
-int batch_word_log2(const trv_task& t) {
-    const uintptr_t a = reinterpret_cast<uintptr_t>(t.src) | reinterpret_cast<uintptr_t>(t.dst);
-    if (t.width % 16 == 0 && (a & 15u) == 0) return 4;
-    if (t.width % 8 == 0 && (a & 7u) == 0) return 3;
-    return 2;
-}
-
-// A batch's plan lives on the device that was current when it was created.
-bool on_batch_device(const trv_batch* b) {
-    int dev = -1;
-    return cudaGetDevice(&dev) == cudaSuccess && dev == b->device;
-}
-
 // Size rule when no tuned tile exists: big enough to amortise the queue
 // step, small enough to balance the tail across 152 SMs.
 int default_tile_bytes(int op) { return op == TRV_OP_COPY ? (128 << 10) : (64 << 10); }
 
-void release(trv_batch* b) {
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->d_tasks) cudaFree(b->d_tasks);
-    if (b->d_prefix) cudaFree(b->d_prefix);
-    if (b->d_counter) cudaFree(b->d_counter);
-    b->exec = nullptr;
-    b->graph = nullptr;
-    b->d_tasks = nullptr;
-    b->d_prefix = nullptr;
-    b->d_counter = nullptr;
+}  // namespace
+
+long long plan_task(int op, uint32_t width, uint64_t n, uint64_t bound, const void* src, void* dst,
+                    const int32_t* idx, const TaskPlan& p, BatchTask* d) {
+    long long tile = (long long)p.tile_bytes / width;
+    tile = tile < 32 ? 32 : (tile / 32) * 32;
+    if (tile > (1 << 30)) tile = 1 << 30;
+    d->src = static_cast<const unsigned char*>(src);
+    d->dst = static_cast<unsigned char*>(dst);
+    d->idx = idx;
+    d->n = (long long)n;
+    d->bound = (long long)bound;
+    d->op = op;
+    d->words = int(width / 4);
+    d->tile_structs = int(tile);
+    // Word moved per lane by the row-form index movers: the widest of 16 / 8
+    // / 4 bytes that divides the width and that both arrays are aligned to.
+    const uintptr_t al = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst);
+    d->word_log2 = (width % 16 == 0 && (al & 15u) == 0) ? 4 : (width % 8 == 0 && (al & 7u) == 0) ? 3 : 2;
+    d->index_mode = op == TRV_OP_GATHER    ? (p.gather_policy == 4 ? 1 : p.gather_policy == 5 ? 2 : 0)
+                    : op == TRV_OP_SCATTER ? (p.scatter_policy == 5 ? 2 : 0)
+                                           : 0;
+    d->copy_bulk = p.copy_bulk;
+    return ((long long)n + tile - 1) / tile;
 }
 
-}  // namespace
+int check_batch_options(const trv_batch_options* opt) {
+    if (!opt) return TRV_OK;
+    if (opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR) return TRV_ERR_UNSUPPORTED;
+    if (opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
+    if (opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4) return TRV_ERR_UNSUPPORTED;
+    if (opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4 && opt->gather_policy != 5)
+        return TRV_ERR_INVALID_ARGUMENT;
+    if (opt->scatter_policy != 0 && opt->scatter_policy != 1 && opt->scatter_policy != 5)
+        return TRV_ERR_INVALID_ARGUMENT;
+    return TRV_OK;
+}
+
+int plan_batch(const trv_task* tasks, uint64_t count, const trv_batch_options* opt, BatchTask* out,
+               long long* prefix, uint64_t* bytes, int* blocks_per_sm) {
+    // bytes of gather / scatter tasks whose tuned entry prefers 2 / 4 blocks per
+    // SM (their movers set the register budget; copy tiles barely use one)
+    uint64_t vote2 = 0, vote4 = 0, total = 0;
+    prefix[0] = 0;
+    for (uint64_t k = 0; k < count; ++k) {
+        const trv_task& t = tasks[k];
+        const int rc = validate(t);
+        if (rc != TRV_OK) return rc;
+        TuneChoice c;
+        const bool tuned = tune_lookup(TuneKey{SCOPE_BATCH, t.op, int(t.width), len_bucket(t.n)}, &c);
+        TaskPlan p;
+        p.tile_bytes = (opt && opt->tile_bytes > 0) ? opt->tile_bytes
+                       : (tuned && c.tile_bytes > 0) ? c.tile_bytes
+                                                     : default_tile_bytes(t.op);
+        // Gather and scatter rows are staged through shared memory with
+        // cp.async unless chosen otherwise: on the 4096-array workload (4
+        // blocks per SM) its gathers took 12.1 ms that way against 20.5 ms
+        // with register-held rows, its scatters 3.5 against 6.3 ms.
+        p.gather_policy = (opt && opt->gather_policy) ? opt->gather_policy
+                          : (tuned && c.cache_policy) ? c.cache_policy
+                                                      : 5;
+        p.scatter_policy = (opt && opt->scatter_policy) ? opt->scatter_policy
+                           : (tuned && c.cache_policy)  ? c.cache_policy
+                                                        : 5;
+        const int cp = (opt && opt->copy_path) ? opt->copy_path : (tuned && c.path) ? c.path : TRV_PATH_AUTO;
+        p.copy_bulk = cp == TRV_PATH_VECTOR ? 0 : 1;
+        prefix[k + 1] = prefix[k] + plan_task(t.op, t.width, t.n, t.bound, t.src, t.dst, t.idx, p, &out[k]);
+        const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
+        total += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 2) vote2 += tb;
+        if (tuned && t.op != TRV_OP_COPY && c.grid == 4) vote4 += tb;
+    }
+    if (bytes) *bytes = total;
+    // One register budget for the whole kernel: the caller's, else the one the
+    // autotuner preferred for most of the batch's bytes, else 4 blocks per SM:
+    // the staged gather / scatter movers and the TMA copy tiles need few
+    // registers, and twice the resident blocks overlap their block barriers
+    // (4096-array workload, default tiles: 22.9 ms against 27.5 ms at 2).
+    *blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote2 > vote4 ? 2 : 4);
+    return TRV_OK;
+}
+
+}  // namespace trv
 
 using namespace trv;
 
@@ -88,59 +166,18 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     *out = nullptr;
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
     if (count >= uint64_t(INT_MAX)) return TRV_ERR_INVALID_ARGUMENT;
-    if (opt && opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR) return TRV_ERR_UNSUPPORTED;
-    if (opt && opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
-    if (opt && opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4)
-        return TRV_ERR_UNSUPPORTED;
-    if (opt && opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4 &&
-        opt->gather_policy != 5)
-        return TRV_ERR_INVALID_ARGUMENT;
+    const int orc = check_batch_options(opt);
+    if (orc != TRV_OK) return orc;
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
     uint64_t bytes = 0;
-    // bytes of gather / scatter tasks whose tuned entry prefers 2 / 4 blocks per
-    // SM (their movers set the register budget; copy tiles barely use one)
-    uint64_t vote2 = 0, vote4 = 0;
-    for (uint64_t k = 0; k < count; ++k) {
-        const trv_task& t = tasks[k];
-        const int rc = validate(t);
-        if (rc != TRV_OK) return rc;
-        TuneChoice c;
-        const TuneKey key{SCOPE_BATCH, t.op, int(t.width), len_bucket(t.n)};
-        const bool tuned = tune_lookup(key, &c);
-        int tile_bytes = (opt && opt->tile_bytes > 0) ? opt->tile_bytes
-                         : (tuned && c.tile_bytes > 0) ? c.tile_bytes
-                                                       : default_tile_bytes(t.op);
-        long long tile = (long long)tile_bytes / t.width;
-        tile = tile < 32 ? 32 : (tile / 32) * 32;
-        if (tile > (1 << 30)) tile = 1 << 30;
-        BatchTask& d = host[k];
-        d.src = static_cast<const unsigned char*>(t.src);
-        d.dst = static_cast<unsigned char*>(t.dst);
-        d.idx = t.idx;
-        d.n = (long long)t.n;
-        d.bound = (long long)t.bound;
-        d.op = t.op;
-        d.words = int(t.width / 4);
-        d.tile_structs = int(tile);
-        d.word_log2 = batch_word_log2(t);
-        // Gather rows are staged through shared memory with cp.async unless
-        // chosen otherwise: on the 4096-array workload its gathers ran 25 %
-        // faster that way (14.9 vs 18.7 ms) than with register-held rows,
-        // whose 128-register kernel keeps only 2 blocks per SM resident.
-        const int gp = (opt && opt->gather_policy) ? opt->gather_policy
-                       : (tuned && c.cache_policy) ? c.cache_policy
-                                                   : 5;
-        d.l2_hint = t.op != TRV_OP_GATHER ? 0 : gp == 4 ? 1 : gp == 5 ? 2 : 0;
-        const int cp = (opt && opt->copy_path) ? opt->copy_path : (tuned && c.path) ? c.path : TRV_PATH_AUTO;
-        d.copy_bulk = cp == TRV_PATH_VECTOR ? 0 : 1;
-        prefix[k + 1] = prefix[k] + (d.n + tile - 1) / tile;
-        const uint64_t tb = 2 * t.n * t.width + (t.op == TRV_OP_COPY ? 0 : 4 * t.n);
-        bytes += tb;
-        if (tuned && t.op != TRV_OP_COPY && c.grid == 2) vote2 += tb;
-        if (tuned && t.op != TRV_OP_COPY && c.grid == 4) vote4 += tb;
-    }
-    if (!device_flag()) return TRV_ERR_CUDA;  // resolved now, outside any later graph capture
+    int blocks_per_sm = 2;
+    const int prc = plan_batch(tasks, count, opt, host.data(), prefix.data(), &bytes, &blocks_per_sm);
+    if (prc != TRV_OK) return prc;
+    // the error flag and the kernel set-up are resolved now, outside any later graph capture
+    if (!device_flag()) return TRV_ERR_CUDA;
+    const int resident = batch_grid(blocks_per_sm);
+    if (resident < 1) return TRV_ERR_CUDA;
     trv_batch* b = new (std::nothrow) trv_batch;
     if (!b) return TRV_ERR_OUT_OF_MEMORY;
     cudaGetDevice(&b->device);
@@ -160,11 +197,7 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
         cudaGetLastError();
         return e == cudaErrorMemoryAllocation ? TRV_ERR_OUT_OF_MEMORY : cuda_fail(e);
     }
-    // One register budget for the whole kernel: the caller's, else the one the
-    // autotuner preferred for most of the batch's bytes, else 2 blocks per SM
-    // (measured faster on the 4096-array workload: no spilled registers).
-    b->blocks_per_sm = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (vote4 > vote2 ? 4 : 2);
-    const int resident = resident_blocks(batch_kernel_func(b->blocks_per_sm), batch_block_threads());
+    b->blocks_per_sm = blocks_per_sm;
     b->grid = (opt && opt->grid_blocks > 0) ? opt->grid_blocks : resident;
     if (b->total_tiles < b->grid) b->grid = b->total_tiles > 0 ? int(b->total_tiles) : 1;
     *out = b;

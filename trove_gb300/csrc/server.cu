@@ -39,6 +39,9 @@ namespace {
 using clock_type = std::chrono::steady_clock;
 
 constexpr uint64_t kGranule = 256;
+// Register budget of the server's batch kernel: 4 resident blocks per SM, the
+// batch default (the staged movers and TMA copy tiles need few registers).
+constexpr int kServerBlocksPerSm = 4;
 
 // First-fit allocator over one device allocation.
 class Arena {
@@ -209,25 +212,15 @@ struct trv_server {
                 const int tb = cfg.tile_bytes > 0 ? cfg.tile_bytes
                                : (tuned && c.tile_bytes > 0) ? c.tile_bytes
                                                              : (r.r.op == TRV_OP_COPY ? (128 << 10) : (64 << 10));
-                long long tile = (long long)tb / r.r.width;
-                tile = tile < 32 ? 32 : (tile / 32) * 32;
-                BatchTask& d = s.h_tasks[k];
-                d.src = static_cast<const unsigned char*>(r.r.src);
-                d.dst = arena.base() + r.off;
-                d.idx = r.r.idx;
-                d.n = (long long)r.r.n;
-                d.bound = (long long)r.r.src_n;
-                d.op = r.r.op;
-                d.words = int(r.r.width / 4);
-                d.tile_structs = int(tile);
-                const uintptr_t al = reinterpret_cast<uintptr_t>(d.src) | reinterpret_cast<uintptr_t>(d.dst);
-                d.word_log2 = (r.r.width % 16 == 0 && (al & 15u) == 0) ? 4
-                              : (r.r.width % 8 == 0 && (al & 7u) == 0) ? 3
-                                                                        : 2;
-                d.l2_hint = r.r.op == TRV_OP_GATHER ? 2 : 0;  // rows staged through shared memory
-                d.copy_bulk = 1;
+                TaskPlan p;
+                p.tile_bytes = tb;
+                p.gather_policy = 5;  // rows staged through shared memory
+                p.scatter_policy = 5;
+                p.copy_bulk = 1;
+                const long long nt = plan_task(r.r.op, r.r.width, r.r.n, r.r.src_n, r.r.src, arena.base() + r.off,
+                                               r.r.idx, p, &s.h_tasks[k]);
                 s.h_prefix[k] = tiles;
-                tiles += (d.n + tile - 1) / tile;
+                tiles += nt;
                 r.phase = LAUNCHED;
                 r.batch = batches;
                 r.launch_ms = t;
@@ -241,7 +234,7 @@ struct trv_server {
             if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), s.stream);
             if (e == cudaSuccess) {
                 const int g = tiles < grid ? int(tiles > 0 ? tiles : 1) : grid;
-                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, 2, s.stream);
+                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, kServerBlocksPerSm, s.stream);
             }
             if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
             if (e != cudaSuccess && error == TRV_OK) error = cuda_fail(e);
@@ -322,7 +315,10 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
     *out = nullptr;
     if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_batch_requests < 0 || cfg->tile_bytes < 0)
         return TRV_ERR_INVALID_ARGUMENT;
-    if (!device_flag()) return TRV_ERR_CUDA;  // the batch kernel's error flag, found before the dispatcher runs
+    // the batch kernel's error flag and set-up, resolved before the dispatcher runs
+    if (!device_flag()) return TRV_ERR_CUDA;
+    const int resident = batch_grid(kServerBlocksPerSm);
+    if (resident < 1) return TRV_ERR_CUDA;
     trv_server* s = new (std::nothrow) trv_server;
     if (!s) return TRV_ERR_OUT_OF_MEMORY;
     s->cfg = *cfg;
@@ -351,7 +347,6 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
         }
     }
     // Concurrent batches share the GPU: each gets an equal part of it.
-    const int resident = resident_blocks(batch_kernel_func(2), batch_block_threads());
     s->grid = std::max(1, resident / s->cfg.max_inflight);
     s->t0 = clock_type::now();
     s->dispatcher = std::thread([s] { s->run(); });
