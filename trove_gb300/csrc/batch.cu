@@ -27,31 +27,35 @@
 namespace trv {
 namespace {
 
-constexpr int kBatchBlock = 256;
-constexpr int kWarps = kBatchBlock / 32;
-
 // Copy tiles whose source and destination are 16-byte aligned move through
 // the TMA bulk engine: one thread streams the tile as kBulkChunk pieces
-// through a ring of kBulkStages shared-memory buffers (load, then store of
-// each piece; a stage is refilled once the store that read it has finished).
-// The bytes in flight then come from shared memory, not from registers,
-// which the kernel's gather / scatter movers already use up (2 resident
-// blocks per SM at 128 registers).
-constexpr int kBulkStages = 4;
+// through a ring of shared-memory stages (load, then store of each piece; a
+// stage is refilled once the store that read it has finished).  The bytes in
+// flight then come from shared memory, not from registers.
 constexpr int kBulkChunk = 8 << 10;
-constexpr int kBulkSmem = kBulkStages * kBulkChunk;
-// Staged gathers and scatters (below) cycle through kStagedPieces buffers of
-// kPieceBytes, each with kIdxSlots index slots.  Two pieces per block: four
-// per block measured slower (18.5 vs 14.9 ms for the 4096-array batch's
-// gathers at 2 blocks per SM); more resident blocks is what pays (11.7 ms at
-// 4 blocks per SM), as block barriers then overlap.  The copy ring reuses the
-// first kBulkSmem bytes of the same buffer.
-constexpr int kPieceBytes = 16 << 10;
-constexpr int kIdxSlots = 1024;
-constexpr int kStagedPieces = 2;
-template <int MINB>
-constexpr int kDynSmem = kStagedPieces * (kPieceBytes + kIdxSlots * int(sizeof(int)));
-static_assert(kBulkSmem <= kStagedPieces * kPieceBytes, "the copy ring fits the piece buffers");
+
+// Launch shapes of the persistent kernel: block size, resident blocks per SM
+// it is built for (hence the register budget), the staged gather / scatter
+// piece with its index slots, and the copy ring's stages.  Staged movers
+// cycle through two pieces per block; four per block measured slower (18.5
+// vs 14.9 ms for the 4096-array batch's gathers at 2 blocks per SM): more
+// resident blocks is what pays (12.1 ms at 4), as block barriers then
+// overlap.  128-thread blocks, 8 per SM, with 8 KiB pieces measured no
+// better (23.8 vs 22.9 ms for the whole batch).  The copy ring reuses the
+// piece buffers.  Either shape holds 160 KiB of shared memory per SM.
+template <int BLOCK, int MINB, int PIECE, int RING>
+struct Shape {
+    static constexpr int block = BLOCK;
+    static constexpr int warps = BLOCK / 32;
+    static constexpr int minb = MINB;
+    static constexpr int piece = PIECE;           // bytes of one staged piece
+    static constexpr int idx_slots = PIECE / 16;  // indices of one staged piece
+    static constexpr int ring = RING;             // copy stages of kBulkChunk bytes
+    static constexpr int dyn_smem = 2 * (PIECE + idx_slots * int(sizeof(int)));
+    static_assert(RING * kBulkChunk <= 2 * PIECE, "the copy ring fits the piece buffers");
+};
+using Shape2 = Shape<256, 2, 16 << 10, 4>;  // 128 registers per thread
+using Shape4 = Shape<256, 4, 16 << 10, 4>;  // 64 registers
 
 // ---- per-tile movers (all warps of the CTA cooperate on one tile) --------
 
@@ -66,6 +70,7 @@ __device__ __forceinline__ int opaque_tid() {
 }
 
 // Flat copy of a byte range with the widest vector both pointers allow.
+template <class S>
 __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned char* d, long long nbytes) {
     const int tid = opaque_tid();
     const unsigned a = unsigned(reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d));
@@ -74,24 +79,24 @@ __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned 
         const long long nv = nbytes >> 4;
         const uint4* sv = reinterpret_cast<const uint4*>(s);
         uint4* dv = reinterpret_cast<uint4*>(d);
-        for (long long k = tid; k < nv; k += 4 * kBatchBlock) {
+        for (long long k = tid; k < nv; k += 4 * S::block) {
             uint4 r[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (k + u * kBatchBlock < nv) r[u] = __ldg(sv + k + u * kBatchBlock);
+                if (k + u * S::block < nv) r[u] = __ldg(sv + k + u * S::block);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (k + u * kBatchBlock < nv) __stcs(dv + k + u * kBatchBlock, r[u]);
+                if (k + u * S::block < nv) __stcs(dv + k + u * S::block, r[u]);
         }
         done = nv << 4;
     } else if ((a & 3u) == 0) {
         const long long nv = nbytes >> 2;
         const unsigned* sv = reinterpret_cast<const unsigned*>(s);
         unsigned* dv = reinterpret_cast<unsigned*>(d);
-        for (long long k = tid; k < nv; k += kBatchBlock) dv[k] = __ldg(sv + k);
+        for (long long k = tid; k < nv; k += S::block) dv[k] = __ldg(sv + k);
         done = nv << 2;
     }
-    for (long long b = done + tid; b < nbytes; b += kBatchBlock) d[b] = s[b];
+    for (long long b = done + tid; b < nbytes; b += S::block) d[b] = s[b];
 }
 
 // TMA bulk copy of one tile by the calling thread (thread 0 of the CTA).
@@ -99,6 +104,7 @@ __device__ __forceinline__ void tile_copy_flat(const unsigned char* s, unsigned 
 // uses stage k % S and completes phase (k / S) & 1 of that stage's
 // mbarrier.  Every wait is bounded; on a timeout the device flag is set, the
 // loads still in flight are drained (bounded) and false is returned.
+template <class S>
 __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long long nbytes, unsigned char* stage,
                                unsigned long long* bar, unsigned long long& seq, int* flag) {
     const long long body = nbytes & ~15ll;
@@ -108,11 +114,11 @@ __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long lo
         return static_cast<unsigned>(body - off < kBulkChunk ? body - off : kBulkChunk);
     };
     auto issue = [&](long long c) {
-        const int st = int((seq + (unsigned long long)c) % kBulkStages);
+        const int st = int((seq + (unsigned long long)c) % S::ring);
         mbar_expect_tx(&bar[st], chunk_bytes(c));
         bulk_load(stage + (size_t)st * kBulkChunk, s + c * kBulkChunk, chunk_bytes(c), &bar[st]);
     };
-    const long long prologue = nchunks < kBulkStages ? nchunks : kBulkStages;
+    const long long prologue = nchunks < S::ring ? nchunks : S::ring;
     fence_proxy_async_shared();  // earlier generic-proxy use of the stages (gather tiles) before TMA writes
     for (long long c = 0; c < prologue; ++c) issue(c);
     long long issued = prologue;
@@ -120,8 +126,8 @@ __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long lo
     long long c = 0;
     for (; c < nchunks; ++c) {
         const unsigned long long k = seq + (unsigned long long)c;
-        const int st = int(k % kBulkStages);
-        if (!mbar_wait(&bar[st], unsigned((k / kBulkStages) & 1))) {
+        const int st = int(k % S::ring);
+        if (!mbar_wait(&bar[st], unsigned((k / S::ring) & 1))) {
             ok = false;
             break;
         }
@@ -136,7 +142,7 @@ __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long lo
         atomicExch(flag, 1);
         for (long long j = c; j < issued; ++j) {
             const unsigned long long k = seq + (unsigned long long)j;
-            mbar_wait(&bar[k % kBulkStages], unsigned((k / kBulkStages) & 1));
+            mbar_wait(&bar[k % S::ring], unsigned((k / S::ring) & 1));
         }
     }
     bulk_wait_read_0();  // stages free for the next tile
@@ -152,13 +158,13 @@ __device__ bool tile_copy_bulk(const unsigned char* s, unsigned char* d, long lo
 // stores).  Round k, lane l: word q = l + 32k of the chunk, i.e. word q % m of
 // struct q / m, whose index comes from that struct's lane by one shuffle.  m is
 // uniform across the warp, so the guarded shuffles are too.
-template <typename V, int U, int G, bool GATHER>
+template <class S, typename V, int U, int G, bool GATHER>
 __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int* idx, long long bound, long long first,
                                                 long long cnt, int m, bool hint) {
     const int tid = opaque_tid();
     const int lane = tid & 31, warp = tid >> 5;
     const long long end = first + cnt;
-    for (long long base = first + warp * 32 * U; base < end; base += kWarps * 32 * U) {
+    for (long long base = first + warp * 32 * U; base < end; base += S::warps * 32 * U) {
         int id[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -207,11 +213,11 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
 // it can be), then write the buffer out to the contiguous destination with
 // coalesced stores.  Scatter: the contiguous source piece is copied in the
 // same way, then each word is stored to its random destination row from
-// shared memory (stores need no registers held in flight either).  D buffers
-// of kPieceBytes rotate, so the copies of the next D - 1 pieces are in flight
-// while the current one is written.  Word q of a piece (words of sizeof(V))
-// belongs to struct q / m; the piece's indices are staged in shared memory
-// first (one coalesced read), invalid ones marked -1.
+// shared memory (stores need no registers held in flight either).  Two
+// buffers of S::piece bytes alternate, so the next piece's copies are in
+// flight while the current one is written.  Word q of a piece (words of
+// sizeof(V)) belongs to struct q / m; the piece's indices are staged in
+// shared memory first (one coalesced read), invalid ones marked -1.
 __device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int bytes) {
     const unsigned s = smem_addr(smem);
     if (bytes == 16)
@@ -234,48 +240,48 @@ __device__ __forceinline__ void cp_async_wait_pending(int n) {
         asm volatile("cp.async.wait_group 3;" ::: "memory");
 }
 
-template <typename V, int D, bool GATHER>
+template <class S, typename V, bool GATHER>
 __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long long bound, long long first,
                                   long long cnt, int m, unsigned char* stage, int* s_idx) {
-    static_assert(D >= 2 && D <= 4, "wait depths 0..3");
+    constexpr int D = 2;
     const int tid = opaque_tid();
     // structs per piece: a multiple of 32 that fits the buffer and the index slots
-    int per = (kPieceBytes / int(sizeof(V))) / m / 32 * 32;
-    if (per > kIdxSlots) per = kIdxSlots;
+    int per = (S::piece / int(sizeof(V))) / m / 32 * 32;
+    if (per > S::idx_slots) per = S::idx_slots;
     // q / m for q < 2^12 and m <= 16 as a multiply and shift (exact there)
     const unsigned inv_m = (65536u + unsigned(m) - 1) / unsigned(m);
     const long long pieces = (cnt + per - 1) / per;
     auto issue = [&](long long p) {
         const int b = int(p % D);
-        V* buf = reinterpret_cast<V*>(stage + b * kPieceBytes);
-        int* ix = s_idx + b * kIdxSlots;
+        V* buf = reinterpret_cast<V*>(stage + b * S::piece);
+        int* ix = s_idx + b * S::idx_slots;
         const long long base = first + p * per;
         const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
-        for (int j = tid; j < n_here; j += kBatchBlock) {
+        for (int j = tid; j < n_here; j += S::block) {
             const int v = __ldcs(idx + base + j);
             ix[j] = (v >= 0 && (long long)v < bound) ? v : -1;
         }
         const int words = n_here * m;
         if (GATHER) {
             __syncthreads();  // the copies below read the staged indices
-            for (int q = tid; q < words; q += kBatchBlock) {
+            for (int q = tid; q < words; q += S::block) {
                 const int j = int((unsigned(q) * inv_m) >> 16);
                 const int v = ix[j];
                 if (v >= 0) cp_async_word(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
             }
         } else {  // indices are next read after the wait's barrier
-            for (int q = tid; q < words; q += kBatchBlock) cp_async_word(buf + q, src + base * m + q, int(sizeof(V)));
+            for (int q = tid; q < words; q += S::block) cp_async_word(buf + q, src + base * m + q, int(sizeof(V)));
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     auto drain = [&](long long p) {
         const int b = int(p % D);
-        const V* buf = reinterpret_cast<const V*>(stage + b * kPieceBytes);
-        const int* ix = s_idx + b * kIdxSlots;
+        const V* buf = reinterpret_cast<const V*>(stage + b * S::piece);
+        const int* ix = s_idx + b * S::idx_slots;
         const long long base = first + p * per;
         const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
         const int words = n_here * m;
-        for (int q = tid; q < words; q += kBatchBlock) {
+        for (int q = tid; q < words; q += S::block) {
             const int j = int((unsigned(q) * inv_m) >> 16);
             const int v = ix[j];
             if (v < 0) continue;
@@ -298,52 +304,51 @@ __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long lon
     }
 }
 
-template <bool GATHER>
+template <class S, bool GATHER>
 __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, long long cnt) {
     const int m = t.words * 4 >> t.word_log2;
     if (t.word_log2 == 4)
-        tile_index_rows<uint4, 2, 2, GATHER>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
+        tile_index_rows<S, uint4, 2, 2, GATHER>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
                                              t.idx, t.bound, first, cnt, m, t.index_mode == 1);
     else if (t.word_log2 == 3)
-        tile_index_rows<uint2, 2, 4, GATHER>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
+        tile_index_rows<S, uint2, 2, 4, GATHER>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
                                              t.idx, t.bound, first, cnt, m, t.index_mode == 1);
     else
-        tile_index_rows<unsigned, 2, 4, GATHER>(reinterpret_cast<const unsigned*>(t.src),
+        tile_index_rows<S, unsigned, 2, 4, GATHER>(reinterpret_cast<const unsigned*>(t.src),
                                                 reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m,
                                                 t.index_mode == 1);
 }
 
-template <bool GATHER>
+template <class S, bool GATHER>
 __device__ __forceinline__ void tile_staged(const BatchTask& t, long long first, long long cnt, int m,
                                             unsigned char* stage, int* s_idx) {
     if (t.word_log2 == 4)
-        tile_index_staged<uint4, kStagedPieces, GATHER>(reinterpret_cast<const uint4*>(t.src),
+        tile_index_staged<S, uint4, GATHER>(reinterpret_cast<const uint4*>(t.src),
                                                         reinterpret_cast<uint4*>(t.dst), t.idx, t.bound, first, cnt,
                                                         m, stage, s_idx);
     else if (t.word_log2 == 3)
-        tile_index_staged<uint2, kStagedPieces, GATHER>(reinterpret_cast<const uint2*>(t.src),
+        tile_index_staged<S, uint2, GATHER>(reinterpret_cast<const uint2*>(t.src),
                                                         reinterpret_cast<uint2*>(t.dst), t.idx, t.bound, first, cnt,
                                                         m, stage, s_idx);
     else
-        tile_index_staged<unsigned, kStagedPieces, GATHER>(reinterpret_cast<const unsigned*>(t.src),
+        tile_index_staged<S, unsigned, GATHER>(reinterpret_cast<const unsigned*>(t.src),
                                                            reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first,
                                                            cnt, m, stage, s_idx);
 }
 
-// MINB resident blocks per SM: 2 gives each thread 128 registers (no
-// spills), 4 gives 64 (a few spilled words, twice the warps for latency
-// hiding); the batch options or the autotuner pick one.
-template <int MINB>
-__global__ void __launch_bounds__(kBatchBlock, MINB)
+// The persistent kernel in launch shape S (Shape2 / Shape4): the batch
+// options or the autotuner pick one.
+template <class S>
+__global__ void __launch_bounds__(S::block, S::minb)
 batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* __restrict__ tile_prefix,
              unsigned long long* counter, int* flag) {
     __shared__ long long s_tile;
-    __shared__ __align__(8) unsigned long long s_bar[kBulkStages];
-    extern __shared__ __align__(128) unsigned char s_stage[];  // kDynSmem<MINB> bytes
-    int* s_idx = reinterpret_cast<int*>(s_stage + kStagedPieces * kPieceBytes);
+    __shared__ __align__(8) unsigned long long s_bar[S::ring];
+    extern __shared__ __align__(128) unsigned char s_stage[];  // S::dyn_smem bytes
+    int* s_idx = reinterpret_cast<int*>(s_stage + 2 * S::piece);
     unsigned long long seq = 0;  // thread 0: bulk loads issued so far
     if (threadIdx.x == 0) {
-        for (int k = 0; k < kBulkStages; ++k) mbar_init(&s_bar[k], 1);
+        for (int k = 0; k < S::ring; ++k) mbar_init(&s_bar[k], 1);
         fence_mbarrier_init();
     }
     __syncthreads();
@@ -373,22 +378,38 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
                               ((reinterpret_cast<uintptr_t>(cs) | reinterpret_cast<uintptr_t>(cd)) & 15u) == 0 &&
                               cnt * w >= 16;
             if (bulk) {
-                if (threadIdx.x == 0) tile_copy_bulk(cs, cd, cnt * w, s_stage, s_bar, seq, flag);
+                if (threadIdx.x == 0) tile_copy_bulk<S>(cs, cd, cnt * w, s_stage, s_bar, seq, flag);
             } else {
-                tile_copy_flat(cs, cd, cnt * w);
+                tile_copy_flat<S>(cs, cd, cnt * w);
             }
         } else if (t.index_mode == 2) {  // gather / scatter staged through shared memory
             const int m = t.words * 4 >> t.word_log2;
             if (t.op == TRV_OP_GATHER)
-                tile_staged<true>(t, first, cnt, m, s_stage, s_idx);
+                tile_staged<S, true>(t, first, cnt, m, s_stage, s_idx);
             else
-                tile_staged<false>(t, first, cnt, m, s_stage, s_idx);
+                tile_staged<S, false>(t, first, cnt, m, s_stage, s_idx);
         } else if (t.op == TRV_OP_GATHER) {
-            tile_index<true>(t, first, cnt);
+            tile_index<S, true>(t, first, cnt);
         } else {
-            tile_index<false>(t, first, cnt);
+            tile_index<S, false>(t, first, cnt);
         }
     }
+}
+
+template <class S>
+bool shape_setup(int* per_sm) {
+    return cudaFuncSetAttribute(batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::dyn_smem) ==
+               cudaSuccess &&
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<S>, S::block, S::dyn_smem) ==
+               cudaSuccess &&
+           *per_sm >= 1;
+}
+
+template <class S>
+cudaError_t launch_shape(const BatchTask* tasks, int ntasks, const long long* tile_prefix,
+                         unsigned long long* counter, int grid, int* flag, cudaStream_t st) {
+    batch_kernel<S><<<grid, S::block, S::dyn_smem, st>>>(tasks, ntasks, tile_prefix, counter, flag);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -403,20 +424,12 @@ int batch_grid(int blocks_per_sm) {
     const int which = blocks_per_sm == 2 ? 0 : 1;
     std::lock_guard<std::mutex> g(mu);
     if (!resident[d.device][0]) {
-        int r2 = 0, r4 = 0;
-        if (cudaFuncSetAttribute(batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem<2>) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(batch_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem<4>) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r2, batch_kernel<2>, kBatchBlock, kDynSmem<2>) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r4, batch_kernel<4>, kBatchBlock, kDynSmem<4>) !=
-                cudaSuccess || r2 < 1 || r4 < 1) {
+        int r[2] = {0, 0};
+        if (!shape_setup<Shape2>(&r[0]) || !shape_setup<Shape4>(&r[1])) {
             cudaGetLastError();
             return 0;
         }
-        resident[d.device][0] = r2 * d.sm_count;
-        resident[d.device][1] = r4 * d.sm_count;
+        for (int k = 0; k < 2; ++k) resident[d.device][k] = r[k] * d.sm_count;
     }
     return resident[d.device][which];
 }
@@ -425,11 +438,8 @@ cudaError_t launch_batch_kernel(const BatchTask* tasks, int ntasks, const long l
                                 unsigned long long* counter, int grid, int blocks_per_sm, cudaStream_t st) {
     int* flag = device_flag();
     if (!flag) return cudaErrorMemoryAllocation;
-    if (blocks_per_sm == 2)
-        batch_kernel<2><<<grid, kBatchBlock, kDynSmem<2>, st>>>(tasks, ntasks, tile_prefix, counter, flag);
-    else
-        batch_kernel<4><<<grid, kBatchBlock, kDynSmem<4>, st>>>(tasks, ntasks, tile_prefix, counter, flag);
-    return cudaGetLastError();
+    if (blocks_per_sm == 2) return launch_shape<Shape2>(tasks, ntasks, tile_prefix, counter, grid, flag, st);
+    return launch_shape<Shape4>(tasks, ntasks, tile_prefix, counter, grid, flag, st);
 }
 
 }  // namespace trv
