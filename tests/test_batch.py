@@ -184,6 +184,50 @@ def test_batch_register_budgets(cuda, blocks_per_sm, policy):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("policy", [1, 5])
+def test_batch_misaligned_arrays(cuda, policy):
+    """Arrays 4 or 8 bytes past a 16-byte boundary (slices of larger buffers):
+    the movers fall back from their 16- and 8-byte words and vectors."""
+    torch = cuda
+    tasks, expect = [], []
+    rng = np.random.default_rng(31)
+    for k, (op, w, n, so, do) in enumerate([(0, 12, 4097, 4, 8), (0, 64, 3000, 8, 4), (1, 16, 5000, 4, 4),
+                                            (1, 64, 2500, 8, 0), (1, 20, 4099, 0, 4), (2, 16, 5000, 4, 8),
+                                            (2, 12, 4096, 8, 4), (2, 64, 1500, 0, 8)]):
+        src_h = oracle.random_structs(n, w, seed=500 + k)
+        sbuf = torch.zeros(n * w + 16, dtype=torch.uint8, device="cuda")
+        sbuf[so:so + n * w] = torch.from_numpy(src_h.reshape(-1).copy()).cuda()
+        dbuf = torch.full((n * w + 16,), SENTINEL, dtype=torch.uint8, device="cuda")
+        init = np.full(n * w, SENTINEL, np.uint8)
+        idx_t = None
+        if op == 0:
+            e = src_h.reshape(-1).copy()
+        elif op == 1:
+            idx_h = rng.integers(0, n, size=n).astype(np.int32)
+            idx_h[11] = -1
+            e = init.reshape(-1, w).copy()
+            ok = idx_h >= 0
+            e[ok] = src_h[idx_h[ok]]
+            e = e.reshape(-1)
+            idx_t = torch.from_numpy(idx_h).cuda()
+        else:
+            idx_h = oracle.permutation(n, 600 + k)
+            e = oracle.scatter(init, src_h, idx_h, n, w)
+            idx_t = torch.from_numpy(idx_h.copy()).cuda()
+        tasks.append(dict(op=op, width=w, n=n, src=sbuf[so:], dst=dbuf[do:], idx=idx_t, bound=n, keep=(sbuf, dbuf, do)))
+        expect.append(e)
+    b = tg.Batch(tasks, gather_policy=policy, scatter_policy=policy)
+    b.launch()
+    torch.cuda.synchronize()
+    for k, (t, e) in enumerate(zip(tasks, expect)):
+        sbuf, dbuf, do = t["keep"]
+        got = dbuf.cpu().numpy()
+        assert np.array_equal(got[do:do + e.size], e), k
+        assert (got[:do] == SENTINEL).all() and (got[do + e.size:] == SENTINEL).all(), k
+    b.close()
+
+
+@pytest.mark.gpu
 def test_batch_grid_override_and_empty(cuda):
     torch = cuda
     tasks, expect = make_workload(torch, 40, seed=5)
