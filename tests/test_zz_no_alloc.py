@@ -69,6 +69,12 @@ def test_static_batch_equals_allocating_batch(cuda):
     torch.cuda.synchronize()
     for got, e in zip(outputs(more), expect):
         assert np.array_equal(got, e)
+    # register-held rows at the 128-register budget, through the same array
+    reset(more)
+    tg.run_static(more, blocks_per_sm=2, gather_policy=1, scatter_policy=1)
+    torch.cuda.synchronize()
+    for got, e in zip(outputs(more), expect):
+        assert np.array_equal(got, e)
 
 
 def test_static_batch_limit(cuda):

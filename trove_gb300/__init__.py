@@ -352,7 +352,8 @@ class Batch:
 STATIC_BATCH_MAX_TASKS = 4096
 
 
-def run_static(tasks, *, tile_bytes: int = 0, grid: int = 0, blocks_per_sm: int = 0, stream=None):
+def run_static(tasks, *, tile_bytes: int = 0, grid: int = 0, blocks_per_sm: int = 0, gather_policy: int = 0,
+               scatter_policy: int = 0, stream=None):
     """Plan and run a batch in one call without allocating device memory
     (trv_batch_run_static), for callers that must not call cudaMalloc: it
     synchronizes the whole device, and a process whose device memory is
@@ -361,7 +362,8 @@ def run_static(tasks, *, tile_bytes: int = 0, grid: int = 0, blocks_per_sm: int 
     shared by every call on the device: calls whose work overlaps on the GPU
     race and must be ordered by the caller."""
     arr = make_tasks(tasks)
-    opt = BatchOptions(int(tile_bytes), PATH_AUTO, int(grid), int(blocks_per_sm))
+    opt = BatchOptions(int(tile_bytes), PATH_AUTO, int(grid), int(blocks_per_sm), int(gather_policy),
+                       int(scatter_policy))
     _check(load().trv_batch_run_static(arr, len(arr), ctypes.byref(opt), _stream(stream)), "trv_batch_run_static")
 
 

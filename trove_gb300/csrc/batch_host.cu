@@ -21,7 +21,7 @@ struct trv_batch {
     long long total_tiles = 0;
     uint64_t bytes = 0;
     int grid = 0;
-    int blocks_per_sm = 2;
+    int blocks_per_sm = 4;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -171,7 +171,7 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1, 0);
     uint64_t bytes = 0;
-    int blocks_per_sm = 2;
+    int blocks_per_sm = 4;
     const int prc = plan_batch(tasks, count, opt, host.data(), prefix.data(), &bytes, &blocks_per_sm);
     if (prc != TRV_OK) return prc;
     // the error flag and the kernel set-up are resolved now, outside any later graph capture

@@ -77,7 +77,7 @@ extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, c
     if (orc != TRV_OK) return orc;
     std::vector<BatchTask> host(count);
     std::vector<long long> prefix(count + 1);
-    int blocks_per_sm = 2;
+    int blocks_per_sm = 4;
     const int rc = plan_batch(tasks, count, opt, host.data(), prefix.data(), nullptr, &blocks_per_sm);
     if (rc != TRV_OK) return rc;
     if (count == 0 || prefix[count] == 0) return TRV_OK;
