@@ -36,6 +36,7 @@ multithreaded port) on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -43,6 +44,7 @@ import statistics
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 from pathlib import Path
 
@@ -128,6 +130,77 @@ def hbm_peak():
     return 6800.0, "fallback"
 
 
+class NvmlClocks:
+    """SM / memory clocks and clock-event reasons read through NVML (the
+    driver's libnvidia-ml, read-only queries) every 2 ms from a background
+    thread while the timed region runs, so regions far shorter than
+    nvidia-smi's sampling period are sampled too.  Raises OSError when NVML
+    or the device cannot be opened."""
+    CLOCK_SM, CLOCK_MEM = 1, 2  # nvmlClockType_t
+    # clock-event reason bits of the NVML API
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, pci_bus_id: str | None, index: int):
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib = lib
+        self.dev = ctypes.c_void_p()
+        rc = -1
+        if pci_bus_id:
+            rc = lib.nvmlDeviceGetHandleByPciBusId_v2(pci_bus_id.encode(), ctypes.byref(self.dev))
+        if rc != 0:
+            rc = lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.dev))
+        if rc != 0:
+            lib.nvmlShutdown()
+            raise OSError("no NVML handle for the device")
+        self.reason_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        mx = ctypes.c_uint(0)
+        self.sm_max = float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(self.dev, self.CLOCK_SM, ctypes.byref(mx)) == 0 \
+            else None
+        self.sm, self.mem, self.reasons = [], [], set()
+        self.stop_flag = threading.Event()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def _run(self):
+        sm, mem, why = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_ulonglong(0)
+        while True:
+            if self.lib.nvmlDeviceGetClockInfo(self.dev, self.CLOCK_SM, ctypes.byref(sm)) == 0:
+                self.sm.append(float(sm.value))
+            if self.lib.nvmlDeviceGetClockInfo(self.dev, self.CLOCK_MEM, ctypes.byref(mem)) == 0:
+                self.mem.append(float(mem.value))
+            if self.reason_fn(self.dev, ctypes.byref(why)) == 0:
+                for bit, name in self.REASONS.items():
+                    if why.value & bit:
+                        self.reasons.add(name)
+            if self.stop_flag.wait(0.002):
+                break
+
+    def stop(self):
+        self.stop_flag.set()
+        self.thread.join()
+        self.lib.nvmlShutdown()
+        return {"sm_mhz": statistics.median(self.sm) if self.sm else None, "sm_max_mhz": self.sm_max,
+                "mem_mhz": statistics.median(self.mem) if self.mem else None, "samples": len(self.sm),
+                "reasons": sorted(self.reasons), "source": "nvml"}
+
+
+def clock_sampler(torch, dev):
+    """NVML poller when the driver's library opens, else nvidia-smi."""
+    index = dev.index or 0
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        bus = "%08x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+    except Exception:
+        bus = None
+    try:
+        return NvmlClocks(bus, index)
+    except (OSError, AttributeError):
+        return Clocks(index)
+
+
 class Clocks:
     """nvidia-smi sampled every 100 ms while the timed region runs (a region
     much shorter than that gets no sample: run it for more steps)."""
@@ -184,7 +257,8 @@ class Clocks:
                     pass
         os.unlink(self.file.name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "mem_mhz": statistics.median(mem) if mem else None, "samples": len(sm), "reasons": sorted(reasons)}
+                "mem_mhz": statistics.median(mem) if mem else None, "samples": len(sm), "reasons": sorted(reasons),
+                "source": "nvidia-smi"}
 
 
 def timed(torch, dev, stream, world, steps, step_fn, label_events=True):
@@ -193,7 +267,7 @@ def timed(torch, dev, stream, world, steps, step_fn, label_events=True):
     torch.cuda.synchronize(dev)
     barrier(world)
     torch.cuda.synchronize(dev)
-    clocks = Clocks(dev.index or 0)
+    clocks = clock_sampler(torch, dev)
     events = [] if label_events else None
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
@@ -1027,7 +1101,7 @@ def run_serve(args, world, rank, local):
     if not args.no_check:
         wl.verify()
     barrier(world)
-    clocks = Clocks(local)
+    clocks = clock_sampler(torch, dev)
     total_bytes, total_ms, stats = wl.run(1.0)
     clock_info = clocks.stop()
     ms = reduce_max(total_ms, world, dev)
