@@ -79,7 +79,8 @@ typedef struct trv_launch {
     int32_t cache_policy;  /* gather / scatter, TRV_PATH_WARP: 0 default; 1 streaming index and
                               contiguous side (evict-first); 2 as 1, random side L2-only;
                               3 as 1, random side kept in L2 (evict-last); 4 as 1, random-side
-                              loads with a 64-byte L2 prefetch-size hint */
+                              loads with a 64-byte L2 prefetch-size hint; 5 as 1, random-side
+                              loads with a 128-byte L2 prefetch-size hint (gathers) */
 } trv_launch;
 
 const char* trv_status_string(int32_t status);
@@ -227,7 +228,8 @@ typedef struct trv_batch_options {
                               0: the autotuned or default choice (4) */
     int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (5);
                               1 plain; 4 with the 64-byte L2 prefetch-size hint; 5 rows staged
-                              through shared memory with asynchronous copies (cp.async) */
+                              through shared memory with asynchronous copies (cp.async); 6 / 7
+                              staged, with the 64 / 128-byte L2 prefetch-size hint */
     int32_t scatter_policy; /* scatter tasks: 0 the autotuned or default choice (5); 1 rows held
                                in registers; 5 the contiguous source staged through shared
                                memory with cp.async, stored to the random rows from there */

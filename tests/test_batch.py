@@ -62,7 +62,7 @@ def test_batch_argument_errors(trove_lib):
     for bad_path in ["bulk", "warp"]:
         with pytest.raises(tg.TroveError):
             tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], copy_path=bad_path)
-    for bad in (dict(gather_policy=2), dict(scatter_policy=4), dict(scatter_policy=-1)):
+    for bad in (dict(gather_policy=2), dict(gather_policy=8), dict(scatter_policy=4), dict(scatter_policy=-1)):
         with pytest.raises(tg.TroveError) as e:
             tg.Batch([dict(op=0, width=12, n=5, src=ok, dst=ok)], **bad)
         assert e.value.status == 1
@@ -129,7 +129,7 @@ def check(tasks, expect):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gather_policy,scatter_policy", [(0, 0), (1, 1), (4, 5), (5, 1), (1, 5)])
+@pytest.mark.parametrize("gather_policy,scatter_policy", [(0, 0), (1, 1), (4, 5), (5, 1), (1, 5), (6, 5), (7, 5)])
 @pytest.mark.parametrize("copy_path", ["vector", "auto"])
 @pytest.mark.parametrize("tile_bytes", [0, 4096, 1 << 20])
 def test_batch_matches_oracle(cuda, copy_path, tile_bytes, gather_policy, scatter_policy):

@@ -80,7 +80,7 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.fill_permutation(0, 5, 0)) == 1
     assert rc_of(lambda: tg.fill_permutation(bad, 5, 0)) == 3
     assert rc_of(lambda: tg.fill_permutation(ok, 0, 0)) == 0
-    assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="warp", policy=5)) == 1
+    assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="warp", policy=6)) == 1
 
 
 def test_error_carries_status_text(trove_lib):

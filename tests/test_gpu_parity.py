@@ -141,7 +141,7 @@ def test_row_form_cache_policies(cuda, width):
     src = to_dev(torch, src_h)
     init = np.full(n * width, SENTINEL, np.uint8)
     sets = index_sets(n, seed=width)
-    for policy in range(5):
+    for policy in range(6):
         for name, idx_h in sets.items():
             idx = torch.from_numpy(idx_h).cuda()
             dst = to_dev(torch, init)
@@ -152,7 +152,7 @@ def test_row_form_cache_policies(cuda, width):
         tg.scatter(dst, n, src, torch.from_numpy(perm_h).cuda(), n, width, path="warp", policy=policy)
         assert np.array_equal(to_host(dst), oracle.scatter(init, src_h, perm_h, n, width)), policy
     with pytest.raises(tg.TroveError):
-        tg.gather(dst, src, n, idx, n, width, path="warp", policy=5)
+        tg.gather(dst, src, n, idx, n, width, path="warp", policy=6)
 
 
 @pytest.mark.parametrize("width", [4, 12, 16, 36, 64])

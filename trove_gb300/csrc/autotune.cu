@@ -172,7 +172,10 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
             for (int u : {1, 2, 4, 8}) cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, 0});
     } else if (width % 4 == 0 && width <= 64) {
         for (int u : {1, 2, 4, 8})
-            for (int cp : {0, 1, 3, 4}) cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, cp});
+            for (int cp : {0, 1, 3, 4, 5}) {
+                if (cp >= 4 && op != TRV_OP_GATHER) continue;  // load hints: a scatter's random side is stores
+                cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, cp});
+            }
         for (int u : {1, 2, 4}) cands.push_back({TRV_PATH_COALESCED, u, 0, 0, 0, 0});
     } else {
         cands.push_back({TRV_PATH_VECTOR, 0, 0, 0, 0, 0});
@@ -238,9 +241,9 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         std::vector<std::tuple<int, int, int, int>> cands;
         for (int tb : {64 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
-                for (int gp : {1, 4, 5})
+                for (int gp : {1, 4, 5, 6, 7})
                     for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
-                        if (gp == 4 && op != TRV_OP_GATHER) continue;  // a load hint
+                        if ((gp == 4 || gp > 5) && op != TRV_OP_GATHER) continue;  // load hints
                         if (gp != 1 && op == TRV_OP_COPY) continue;
                         if (cpath == TRV_PATH_VECTOR && op != TRV_OP_COPY) continue;
                         // the register budget is one per batch and set by its

@@ -217,15 +217,35 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
 // buffers of S::piece bytes alternate, so the next piece's copies are in
 // flight while the current one is written.  Word q of a piece (words of
 // sizeof(V)) belongs to struct q / m; the piece's indices are staged in
-// shared memory first (one coalesced read), invalid ones marked -1.
+// shared memory first (one coalesced read), invalid ones marked -1.  PF is
+// the L2 prefetch size the random row copies ask for on a miss: 0 the
+// context's fetch granularity, 64 or 128 bytes (boxes differ in their
+// default, and the best size depends on the struct width).
+template <int PF>
 __device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int bytes) {
     const unsigned s = smem_addr(smem);
-    if (bytes == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-    else if (bytes == 8)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    if (PF == 64) {
+        if (bytes == 16)
+            asm volatile("cp.async.cg.shared.global.L2::64B [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+        else if (bytes == 8)
+            asm volatile("cp.async.ca.shared.global.L2::64B [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global.L2::64B [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    } else if (PF == 128) {
+        if (bytes == 16)
+            asm volatile("cp.async.cg.shared.global.L2::128B [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+        else if (bytes == 8)
+            asm volatile("cp.async.ca.shared.global.L2::128B [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global.L2::128B [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    } else {
+        if (bytes == 16)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+        else if (bytes == 8)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    }
 }
 
 // Waits until at most n of this thread's cp.async groups are pending.
@@ -240,7 +260,7 @@ __device__ __forceinline__ void cp_async_wait_pending(int n) {
         asm volatile("cp.async.wait_group 3;" ::: "memory");
 }
 
-template <class S, typename V, bool GATHER>
+template <class S, typename V, bool GATHER, int PF>
 __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long long bound, long long first,
                                   long long cnt, int m, unsigned char* stage, int* s_idx) {
     constexpr int D = 2;
@@ -267,10 +287,11 @@ __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long lon
             for (int q = tid; q < words; q += S::block) {
                 const int j = int((unsigned(q) * inv_m) >> 16);
                 const int v = ix[j];
-                if (v >= 0) cp_async_word(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
+                if (v >= 0) cp_async_word<PF>(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
             }
         } else {  // indices are next read after the wait's barrier
-            for (int q = tid; q < words; q += S::block) cp_async_word(buf + q, src + base * m + q, int(sizeof(V)));
+            for (int q = tid; q < words; q += S::block)
+                cp_async_word<0>(buf + q, src + base * m + q, int(sizeof(V)));
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -319,21 +340,35 @@ __device__ __forceinline__ void tile_index(const BatchTask& t, long long first, 
                                                 t.index_mode == 1);
 }
 
-template <class S, bool GATHER>
-__device__ __forceinline__ void tile_staged(const BatchTask& t, long long first, long long cnt, int m,
-                                            unsigned char* stage, int* s_idx) {
+template <class S, bool GATHER, int PF>
+__device__ __forceinline__ void tile_staged_pf(const BatchTask& t, long long first, long long cnt, int m,
+                                               unsigned char* stage, int* s_idx) {
     if (t.word_log2 == 4)
-        tile_index_staged<S, uint4, GATHER>(reinterpret_cast<const uint4*>(t.src),
-                                                        reinterpret_cast<uint4*>(t.dst), t.idx, t.bound, first, cnt,
-                                                        m, stage, s_idx);
+        tile_index_staged<S, uint4, GATHER, PF>(reinterpret_cast<const uint4*>(t.src), reinterpret_cast<uint4*>(t.dst),
+                                                t.idx, t.bound, first, cnt, m, stage, s_idx);
     else if (t.word_log2 == 3)
-        tile_index_staged<S, uint2, GATHER>(reinterpret_cast<const uint2*>(t.src),
-                                                        reinterpret_cast<uint2*>(t.dst), t.idx, t.bound, first, cnt,
-                                                        m, stage, s_idx);
+        tile_index_staged<S, uint2, GATHER, PF>(reinterpret_cast<const uint2*>(t.src), reinterpret_cast<uint2*>(t.dst),
+                                                t.idx, t.bound, first, cnt, m, stage, s_idx);
     else
-        tile_index_staged<S, unsigned, GATHER>(reinterpret_cast<const unsigned*>(t.src),
-                                                           reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first,
-                                                           cnt, m, stage, s_idx);
+        tile_index_staged<S, unsigned, GATHER, PF>(reinterpret_cast<const unsigned*>(t.src),
+                                                   reinterpret_cast<unsigned*>(t.dst), t.idx, t.bound, first, cnt, m,
+                                                   stage, s_idx);
+}
+
+// index_mode 2: staged with the context's fetch size; 3 / 4 (gathers): with
+// the 64 / 128-byte L2 prefetch-size hint.
+template <class S>
+__device__ __forceinline__ void tile_staged(const BatchTask& t, long long first, long long cnt, unsigned char* stage,
+                                            int* s_idx) {
+    const int m = t.words * 4 >> t.word_log2;
+    if (t.op != TRV_OP_GATHER)
+        tile_staged_pf<S, false, 0>(t, first, cnt, m, stage, s_idx);
+    else if (t.index_mode == 3)
+        tile_staged_pf<S, true, 64>(t, first, cnt, m, stage, s_idx);
+    else if (t.index_mode == 4)
+        tile_staged_pf<S, true, 128>(t, first, cnt, m, stage, s_idx);
+    else
+        tile_staged_pf<S, true, 0>(t, first, cnt, m, stage, s_idx);
 }
 
 // The persistent kernel in launch shape S (Shape2 / Shape4): the batch
@@ -382,12 +417,8 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
             } else {
                 tile_copy_flat<S>(cs, cd, cnt * w);
             }
-        } else if (t.index_mode == 2) {  // gather / scatter staged through shared memory
-            const int m = t.words * 4 >> t.word_log2;
-            if (t.op == TRV_OP_GATHER)
-                tile_staged<S, true>(t, first, cnt, m, s_stage, s_idx);
-            else
-                tile_staged<S, false>(t, first, cnt, m, s_stage, s_idx);
+        } else if (t.index_mode >= 2) {  // gather / scatter staged through shared memory
+            tile_staged<S>(t, first, cnt, s_stage, s_idx);
         } else if (t.op == TRV_OP_GATHER) {
             tile_index<S, true>(t, first, cnt);
         } else {

@@ -23,14 +23,16 @@ struct alignas(16) BatchTask {
     int word_log2;    // gather / scatter: log2 of the word moved per lane (2, 3 or 4)
     int index_mode;   // gather / scatter: 0 = rows held in registers, 1 = the same with the 64-byte
                       // L2 prefetch-size hint on random loads (gather), 2 = rows staged through
-                      // shared memory with cp.async
+                      // shared memory with cp.async, 3 / 4 = staged with the 64 / 128-byte hint
+                      // (gather)
     int copy_bulk;    // copy: 1 = TMA bulk tiles where 16-byte aligned, 0 = flat vector tiles
 };
 
 // Per-task choices that are not in the task itself.
 struct TaskPlan {
     int tile_bytes;           // tile size in bytes of structs (rounded to 32 structs)
-    int gather_policy;        // 1 plain, 4 L2 prefetch-size hint, 5 staged through shared memory
+    int gather_policy;        // 1 plain, 4 64-byte L2 prefetch-size hint, 5 staged through shared
+                              // memory, 6 / 7 staged with the 64 / 128-byte hint
     int scatter_policy;       // 1 plain, 5 staged through shared memory
     int copy_bulk;            // copy tiles through the TMA bulk engine where aligned
 };

@@ -92,7 +92,9 @@ long long plan_task(int op, uint32_t width, uint64_t n, uint64_t bound, const vo
     // / 4 bytes that divides the width and that both arrays are aligned to.
     const uintptr_t al = reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst);
     d->word_log2 = (width % 16 == 0 && (al & 15u) == 0) ? 4 : (width % 8 == 0 && (al & 7u) == 0) ? 3 : 2;
-    d->index_mode = op == TRV_OP_GATHER    ? (p.gather_policy == 4 ? 1 : p.gather_policy == 5 ? 2 : 0)
+    d->index_mode = op == TRV_OP_GATHER    ? (p.gather_policy == 4   ? 1
+                                              : p.gather_policy >= 5 ? p.gather_policy - 3
+                                                                     : 0)
                     : op == TRV_OP_SCATTER ? (p.scatter_policy == 5 ? 2 : 0)
                                            : 0;
     d->copy_bulk = p.copy_bulk;
@@ -104,7 +106,7 @@ int check_batch_options(const trv_batch_options* opt) {
     if (opt->copy_path != TRV_PATH_AUTO && opt->copy_path != TRV_PATH_VECTOR) return TRV_ERR_UNSUPPORTED;
     if (opt->tile_bytes < 0) return TRV_ERR_INVALID_ARGUMENT;
     if (opt->blocks_per_sm != 0 && opt->blocks_per_sm != 2 && opt->blocks_per_sm != 4) return TRV_ERR_UNSUPPORTED;
-    if (opt->gather_policy != 0 && opt->gather_policy != 1 && opt->gather_policy != 4 && opt->gather_policy != 5)
+    if (opt->gather_policy != 0 && opt->gather_policy != 1 && (opt->gather_policy < 4 || opt->gather_policy > 7))
         return TRV_ERR_INVALID_ARGUMENT;
     if (opt->scatter_policy != 0 && opt->scatter_policy != 1 && opt->scatter_policy != 5)
         return TRV_ERR_INVALID_ARGUMENT;

@@ -347,7 +347,7 @@ static int32_t index_op(bool gather, void* dst, const void* src, uint64_t bound,
         else
             c.path = wide_words ? TRV_PATH_WARP : TRV_PATH_VECTOR;
     }
-    if (c.cache_policy < 0 || c.cache_policy > 4) return TRV_ERR_INVALID_ARGUMENT;
+    if (c.cache_policy < 0 || c.cache_policy > 5) return TRV_ERR_INVALID_ARGUMENT;
     const int path = c.path;
     const int grid_req = c.grid_blocks;
     if (path == TRV_PATH_VECTOR) {  // generic byte-wise form
