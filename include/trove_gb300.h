@@ -226,7 +226,7 @@ typedef struct trv_batch_options {
     int32_t blocks_per_sm; /* resident blocks per SM: 4 (64 registers per thread) or 2 (128, for
                               the register-held gather / scatter rows of policy 1 and 4);
                               0: the autotuned or default choice (4) */
-    int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (5);
+    int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (7);
                               1 plain; 4 with the 64-byte L2 prefetch-size hint; 5 rows staged
                               through shared memory with asynchronous copies (cp.async); 6 / 7
                               staged, with the 64 / 128-byte L2 prefetch-size hint */

@@ -214,7 +214,7 @@ struct trv_server {
                                                              : (r.r.op == TRV_OP_COPY ? (128 << 10) : (64 << 10));
                 TaskPlan p;
                 p.tile_bytes = tb;
-                p.gather_policy = 5;  // rows staged through shared memory
+                p.gather_policy = 7;  // rows staged through shared memory, 128-byte L2 fetches
                 p.scatter_policy = 5;
                 p.copy_bulk = 1;
                 const long long nt = plan_task(r.r.op, r.r.width, r.r.n, r.r.src_n, r.r.src, arena.base() + r.off,
