@@ -347,8 +347,9 @@ int32_t trv_server_destroy(trv_server* s);
 /* ---- autotuner -------------------------------------------------------------
  * Launch choices cached per (scope, op, width, length bucket of a factor 4).
  * Scope 0 (per call) steers the AUTO path of trv_copy / trv_gather /
- * trv_scatter; scope 1 (batch) gives the batched kernel its tile size and copy
- * variant.  No reference counterpart. */
+ * trv_scatter (path, unroll and cache policy); scope 1 (batch) gives the
+ * batched kernel its tile size, register budget, gather / scatter policy and
+ * copy variant per group.  No reference counterpart. */
 
 /* Times every candidate launch shape for (op, width, n) on scratch arrays of
  * n structs, each run after an L2 flush, median of three (uniform random
@@ -356,16 +357,18 @@ int32_t trv_server_destroy(trv_server* s);
  * TRV_OP_COPY_EXIT_WARP / _BLOCK, tuned with the exit modulus 625, or
  * TRV_OP_AOS_TO_SOA / TRV_OP_SOA_TO_AOS) and caches the fastest in scope 0. */
 int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream);
-/* Times tile sizes for each (op, width, bucket) group of the given tasks,
- * running each group alone as a batch, and caches the fastest in scope 1.
- * The tasks' arrays are read and written. */
+/* Times tile size, register budget, gather / scatter policy and copy variant
+ * for each (op, width, bucket) group of the given tasks, running each group
+ * alone as a batch, and caches the fastest in scope 1.  The tasks' arrays
+ * are read and written. */
 int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream);
 /* Cached choice for (scope, op, width, n); TRV_ERR_NOT_FOUND if none. */
 int32_t trv_autotune_lookup(int32_t scope, int32_t op, uint32_t width, uint64_t n, trv_launch* out,
                             int32_t* tile_bytes);
 int32_t trv_autotune_clear(void);
 /* JSON file: an array of {scope, op, width, bucket, path, unroll, grid, chunk,
- * tile_bytes, gbs} objects. */
+ * tile_bytes, cache_policy, gbs} objects (scope 1 keeps the register budget in
+ * grid and the gather / scatter policy in cache_policy). */
 int32_t trv_autotune_save(const char* path);
 int32_t trv_autotune_load(const char* path);
 
