@@ -80,7 +80,10 @@ typedef struct trv_launch {
                               contiguous side (evict-first); 2 as 1, random side L2-only;
                               3 as 1, random side kept in L2 (evict-last); 4 as 1, random-side
                               loads with a 64-byte L2 prefetch-size hint; 5 as 1, random-side
-                              loads with a 128-byte L2 prefetch-size hint (gathers) */
+                              loads with a 128-byte L2 prefetch-size hint (gathers); 6 (scatters)
+                              as 1, in passes over 64 MiB parts of the destination, so that
+                              partial-sector writes of narrow structs merge in L2 (the default
+                              for structs of at most 16 bytes onto destinations above 64 MiB) */
 } trv_launch;
 
 const char* trv_status_string(int32_t status);

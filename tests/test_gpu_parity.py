@@ -147,12 +147,47 @@ def test_row_form_cache_policies(cuda, width):
             dst = to_dev(torch, init)
             tg.gather(dst, src, n, idx, n, width, path="warp", policy=policy)
             assert np.array_equal(to_host(dst), oracle.gather(init, src_h, idx_h, n, width)), (policy, name)
-        perm_h = sets["perm"]
+    perm_h = sets["perm"]
+    for policy in range(7):
         dst = to_dev(torch, init)
         tg.scatter(dst, n, src, torch.from_numpy(perm_h).cuda(), n, width, path="warp", policy=policy)
         assert np.array_equal(to_host(dst), oracle.scatter(init, src_h, perm_h, n, width)), policy
     with pytest.raises(tg.TroveError):
         tg.gather(dst, src, n, idx, n, width, path="warp", policy=6)
+    with pytest.raises(tg.TroveError):
+        tg.scatter(dst, n, src, torch.from_numpy(perm_h).cuda(), n, width, path="warp", policy=7)
+
+
+@pytest.mark.parametrize("width", [8, 12, 20, 24])
+def test_scatter_destination_passes(cuda, width):
+    """Scatters onto destinations above 64 MiB in destination passes (cache
+    policy 6; the default for structs of at most 16 bytes): every row lands
+    once, skipped indices leave the destination alone, a partial scatter
+    keeps the rest."""
+    torch = cuda
+    n = (1 << 23) + 17  # 8-24 B: 64-192 MiB destinations, 2-3 passes
+    src_h = oracle.random_structs(n, width, seed=width + 40)
+    src = to_dev(torch, src_h)
+    idx_h = oracle.permutation(n, width + 41)
+    idx_h[5] = -1
+    idx_h[77] = n + 3
+    ok = (idx_h >= 0) & (idx_h < n)
+    expect = np.full((n, width), SENTINEL, np.uint8)
+    expect[idx_h[ok]] = src_h[ok]
+    idx = torch.from_numpy(idx_h).cuda()
+    for kw in ({}, {"path": "warp", "policy": 6}, {"path": "warp", "policy": 1}):
+        dst = torch.full((n * width,), SENTINEL, dtype=torch.uint8, device="cuda")
+        tg.scatter(dst, n, src, idx, n, width, **kw)
+        assert np.array_equal(to_host(dst).reshape(n, width), expect), kw
+    # a third of the rows, in passes on request
+    m = n // 3
+    expect = np.full((n, width), SENTINEL, np.uint8)
+    sel = idx_h[:m]
+    okm = (sel >= 0) & (sel < n)
+    expect[sel[okm]] = src_h[:m][okm]
+    dst = torch.full((n * width,), SENTINEL, dtype=torch.uint8, device="cuda")
+    tg.scatter(dst, n, src, idx, m, width, path="warp", policy=6)
+    assert np.array_equal(to_host(dst).reshape(n, width), expect)
 
 
 @pytest.mark.parametrize("width", [4, 12, 16, 36, 64])

@@ -172,8 +172,9 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
             for (int u : {1, 2, 4, 8}) cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, 0});
     } else if (width % 4 == 0 && width <= 64) {
         for (int u : {1, 2, 4, 8})
-            for (int cp : {0, 1, 3, 4, 5}) {
-                if (cp >= 4 && op != TRV_OP_GATHER) continue;  // load hints: a scatter's random side is stores
+            for (int cp : {0, 1, 3, 4, 5, 6}) {
+                if ((cp == 4 || cp == 5) && op != TRV_OP_GATHER) continue;  // load hints: a scatter's random side is stores
+                if (cp == 6 && op != TRV_OP_SCATTER) continue;              // destination passes
                 cands.push_back({TRV_PATH_WARP, u, 0, 0, 0, cp});
             }
         for (int u : {1, 2, 4}) cands.push_back({TRV_PATH_COALESCED, u, 0, 0, 0, 0});

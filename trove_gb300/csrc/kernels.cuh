@@ -407,8 +407,8 @@ gather_rows_kernel(const V* __restrict__ src, long long src_n, const int* __rest
 
 template <int S, typename V, int U>
 __global__ void __launch_bounds__(256)
-scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* __restrict__ dst, long long dst_n,
-                    long long n, int policy) {
+scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* __restrict__ dst, long long dst_lo,
+                    long long dst_hi, long long n, int policy) {
     constexpr int m = S * 4 / int(sizeof(V));
     const WarpGrid g;
     constexpr int CH = 32 * U;
@@ -419,7 +419,7 @@ scatter_rows_kernel(const V* __restrict__ src, const int* __restrict__ idx, V* _
         for (int u = 0; u < U; ++u) {
             const long long i = base + u * 32 + g.lane;
             const int v = i < n ? ld_index(idx + i, policy) : -1;
-            id[u] = (v >= 0 && (long long)v < dst_n) ? v : -1;
+            id[u] = ((long long)v >= dst_lo && (long long)v < dst_hi) ? v : -1;  // dst_lo >= 0
         }
         V val[U][m];
         int to[U][m];

@@ -24,6 +24,7 @@ struct IndexArgs {
     long long n;
     long long bound;  // src_n for gather, dst_n for scatter
     int policy;       // cache policy of the row-form kernels
+    long long lo = 0; // row-form scatter: only destinations in [lo, bound) are written
 };
 
 template <typename Args>

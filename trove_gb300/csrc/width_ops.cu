@@ -71,7 +71,7 @@ void launch_gather_rows(const IndexArgs& a, int grid, int block, cudaStream_t st
 template <typename V, int U>
 void launch_scatter_rows(const IndexArgs& a, int grid, int block, cudaStream_t st) {
     scatter_rows_kernel<S, V, U><<<grid, block, 0, st>>>(static_cast<const V*>(a.src), a.idx,
-                                                         static_cast<V*>(a.dst), a.bound, a.n, a.policy);
+                                                         static_cast<V*>(a.dst), a.lo, a.bound, a.n, a.policy);
 }
 
 template <typename V, int k>
