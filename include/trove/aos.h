@@ -128,6 +128,45 @@ TROVE_D void contiguous_store(const T& data, T* dst) {
 // of m separate per-lane accesses; the rounds are the row form of the
 // transposition, which converts them to one struct per lane (and back for
 // stores).
+// The random-row loads of gather_rows_load carry a 64-byte L2 prefetch-size
+// hint for structs of 20 bytes and more (otherwise they are ordinary coherent
+// loads): on a miss, L2 fetches the 64-byte half line holding the word instead
+// of a whole 128-byte line on GPUs whose default fetch is a whole line, which
+// halves the DRAM bytes read for structs scattered at random.  Measured on a
+// GB300 through coalesced_ptr gathers of 2^24 structs: runs of 32 +4.5 to
+// +11 % from 20 bytes up, permutations +2.5 to +6.6 % from 28 bytes up, but
+// 12-byte permutations -7.5 %, so narrower structs keep plain loads.
+TROVE_D int load_row_word(const int* p) {
+#if defined(__CUDA_ARCH__)
+    int v;
+    asm volatile("ld.global.L2::64B.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+#else
+    return *p;
+#endif
+}
+TROVE_D int2 load_row_word(const int2* p) {
+#if defined(__CUDA_ARCH__)
+    int2 v;
+    asm volatile("ld.global.L2::64B.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
+    return v;
+#else
+    return *p;
+#endif
+}
+TROVE_D int4 load_row_word(const int4* p) {
+#if defined(__CUDA_ARCH__)
+    int4 v;
+    asm volatile("ld.global.L2::64B.v4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+#else
+    return *p;
+#endif
+}
+
 template <typename U, typename T>
 TROVE_D T gather_rows_load(const T* src) {
     constexpr int m = aliased_size<T, U>::value;
@@ -138,7 +177,11 @@ TROVE_D T gather_rows_load(const T* src) {
         const int q = lane + 32 * k;
         const int j = q / m;
         const T* pj = shfl_any(src, j, 0xFFFFFFFFu, 32);
-        r.v[k] = reinterpret_cast<const U*>(pj)[q - j * m];
+        const U* w = reinterpret_cast<const U*>(pj) + (q - j * m);
+        if constexpr (sizeof(T) >= 20)
+            r.v[k] = load_row_word(w);
+        else
+            r.v[k] = *w;
     }
     r2c_block(r, thread_tile<32>());
     return fuse_regs<T>(r);
