@@ -188,7 +188,7 @@ class NvmlClocks:
 
 
 def clock_sampler(torch, dev):
-    """NVML poller when the driver's library opens, else nvidia-smi."""
+    """NVML poller when NVIDIA's management library opens, else nvidia-smi."""
     index = dev.index or 0
     try:
         p = torch.cuda.get_device_properties(dev)

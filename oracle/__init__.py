@@ -1,7 +1,7 @@
 """CPU oracle for the AoS hot path — TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-package, and only as the checker (or, for the baseline, as the timed CPU
+package, and only to verify results (or, for the baseline, as the timed CPU
 form).  The product library never imports it.
 
   * the C restatement (aos_oracle.c) through ctypes: seeded inputs, copy,

@@ -2,7 +2,7 @@
  * CPU oracle for AoS copy / gather / scatter — TEST INFRASTRUCTURE ONLY.
  *
  * Plain C restatement of what the reference's hot path computes, used by the
- * test suite as the bit-exact checker, by __graft_entry__.smoke(), and by
+ * test suite as the bit-exact reference result, by __graft_entry__.smoke(), and by
  * bench.py's CPU baseline.  Nothing in the product links or calls it.
  *
  * The reference is a device-only template library; its semantics on the hot

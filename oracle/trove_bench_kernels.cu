@@ -1,5 +1,5 @@
 // Trove-API kernels in the style of the reference's own tests — TEST
-// INFRASTRUCTURE ONLY (checker and comparison baseline, never the product).
+// INFRASTRUCTURE ONLY (parity tests and comparison baseline, never the product).
 //
 // The same source is compiled against two header trees by
 // oracle/build_oracle.py:

@@ -9,8 +9,8 @@ oracle would take minutes at these sizes):
 * AoS -> SoA -> AoS round trip on 2 GiB;
 * the batched kernel on arrays drawn like the 4096-array workload (lengths
   log-uniform up to 2^22 structs), against per-array torch results.
-Inputs come from the library's seeded generators; torch on the GPU is the
-checker here.
+Inputs come from the library's seeded generators; torch on the GPU computes
+the expected results here.
 """
 import math
 
