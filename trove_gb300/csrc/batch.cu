@@ -219,7 +219,7 @@ __device__ __forceinline__ void tile_index_rows(const V* src, V* dst, const int*
 // sizeof(V)) belongs to struct q / m; the piece's indices are staged in
 // shared memory first (one coalesced read), invalid ones marked -1.  PF is
 // the L2 prefetch size the random row copies ask for on a miss: 0 the
-// context's fetch granularity, 64 or 128 bytes (boxes differ in their
+// context's fetch granularity, 64 or 128 bytes (GB300s differ in their
 // default, and the best size depends on the struct width).
 template <int PF>
 __device__ __forceinline__ void cp_async_word(void* smem, const void* gmem, int bytes) {
