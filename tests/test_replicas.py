@@ -62,3 +62,19 @@ def test_reference_arm_under_torchrun_prints_once(trove_lib):
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_clock_sampler_without_a_gpu():
+    """The timed region's clock record degrades to a reasoned null when
+    neither NVML nor nvidia-smi can be opened (as on a machine without a
+    GPU), instead of failing the run."""
+    import torch
+    sys.path.insert(0, str(ROOT))
+    import bench
+    c = bench.clock_sampler(torch, torch.device("cuda", 0))
+    rec = c.stop()
+    assert set(rec) >= {"sm_mhz", "sm_max_mhz", "reasons"}
+    if rec.get("source") == "nvml":  # a machine with a GPU: real samples
+        assert rec["samples"] >= 1 and rec["sm_mhz"] > 0
+    elif rec["sm_mhz"] is None:
+        assert rec["reasons"] == ["nvidia-smi unavailable"] or rec.get("samples") == 0
