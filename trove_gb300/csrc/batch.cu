@@ -371,6 +371,24 @@ __device__ __forceinline__ void tile_staged(const BatchTask& t, long long first,
         tile_staged_pf<S, true, 0>(t, first, cnt, m, stage, s_idx);
 }
 
+// Task of tile number `tile`: the last k with prefix[k] <= tile (tasks without
+// tiles repeat a prefix value and are skipped).  Each warp searches on its own,
+// 32 probes per round (3 dependent loads for 4096 tasks instead of 12).
+__device__ __forceinline__ int find_task(const long long* __restrict__ prefix, int ntasks, long long tile) {
+    const int lane = opaque_tid() & 31;
+    int lo = 0, hi = ntasks;  // prefix[lo] <= tile < prefix[hi]
+    while (hi - lo > 1) {
+        const int step = (hi - lo + 31) >> 5;
+        const int p = lo + (lane + 1) * step;
+        const bool le = p < hi && __ldg(prefix + p) <= tile;  // true on a prefix of the lanes
+        const int k = __popc(__ballot_sync(0xFFFFFFFFu, le));
+        const int next_hi = lo + (k + 1) * step;
+        lo += k * step;
+        hi = next_hi < hi ? next_hi : hi;
+    }
+    return lo;
+}
+
 // The persistent kernel in launch shape S (Shape2 / Shape4): the batch
 // options or the autotuner pick one.
 template <class S>
@@ -394,14 +412,7 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
         const long long tile = s_tile;
         __syncthreads();
         if (tile >= total) break;
-        int lo = 0, hi = ntasks;  // tile_prefix[lo] <= tile < tile_prefix[hi]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(tile_prefix + mid) <= tile)
-                lo = mid;
-            else
-                hi = mid;
-        }
+        const int lo = find_task(tile_prefix, ntasks, tile);
         const BatchTask& t = tasks[lo];
         const long long first = (tile - __ldg(tile_prefix + lo)) * t.tile_structs;
         const long long cnt = t.n - first < t.tile_structs ? t.n - first : t.tile_structs;
