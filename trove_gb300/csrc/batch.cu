@@ -295,19 +295,20 @@ __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long lon
         int* ix = s_idx + b * S::idx_slots;
         const long long base = first + p * per;
         const int n_here = int(cnt - p * per < per ? cnt - p * per : per);
-        for (int j = tid; j < n_here; j += S::block) {
-            const int v = __ldcs(idx + base + j);
-            ix[j] = (v >= 0 && (long long)v < bound) ? v : -1;
-        }
         const int words = n_here * m;
         if (GATHER) {
+            for (int j = tid; j < n_here; j += S::block) {
+                const int v = __ldcs(idx + base + j);
+                ix[j] = (v >= 0 && (long long)v < bound) ? v : -1;
+            }
             __syncthreads();  // the copies below read the staged indices
             for (int q = tid; q < words; q += S::block) {
                 const int j = int((unsigned(q) * inv_m) >> 16);
                 const int v = ix[j];
                 if (v >= 0) cp_async_word<PF>(buf + q, src + (long long)v * m + (q - j * m), int(sizeof(V)));
             }
-        } else {  // indices are next read after the wait's barrier
+        } else {  // raw indices and source words, both read after the wait's barrier
+            cp_async_range<S>(ix, idx + base, n_here * 4, tid);
             cp_async_range<S>(buf, src + base * m, words * int(sizeof(V)), tid);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
@@ -322,7 +323,7 @@ __device__ void tile_index_staged(const V* src, V* dst, const int* idx, long lon
         for (int q = tid; q < words; q += S::block) {
             const int j = int((unsigned(q) * inv_m) >> 16);
             const int v = ix[j];
-            if (v < 0) continue;
+            if (v < 0 || (!GATHER && (long long)v >= bound)) continue;  // gather slots hold -1 when invalid
             if (GATHER)
                 __stcs(dst + base * m + q, buf[q]);
             else
