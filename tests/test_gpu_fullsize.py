@@ -144,3 +144,27 @@ def test_batch_full_length_distribution(cuda):
             ok = torch.equal(d[t["idx"].long()], s)
         assert ok, (k, t["op"], w, n)
     b.close()
+
+
+def test_copy_beyond_2_31_structs(cuda):
+    """More than 2^31 structs (4-byte, 8.6 GB a side) through trv_copy's default
+    path, the flat vector and warp-contiguous paths and a batch copy task:
+    every offset is 64-bit."""
+    torch = cuda
+    n = (1 << 31) + 4099
+    src = torch.empty(n * 4, dtype=torch.uint8, device="cuda")
+    tg.fill_random_u32(src, n, seed=12)
+    dst = torch.empty_like(src)
+    for kw in ({}, {"path": "vector"}, {"path": "warp"}):
+        dst.zero_()
+        tg.copy(dst, src, n, 4, **kw)
+        torch.cuda.synchronize()
+        assert torch.equal(dst, src), kw
+    dst.zero_()
+    b = tg.Batch([dict(op=tg.OP_COPY, width=4, n=n, src=src, dst=dst)])
+    b.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(dst, src)
+    b.close()
+    del src, dst
+    torch.cuda.empty_cache()
