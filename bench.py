@@ -1183,7 +1183,11 @@ def run_trove(args, world, rank, local):
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["gbs"], "peak": peak,
                      "unit": "GB/s", "frac": top["frac"], "traffic": traffic,
                      "bytes_per_launch": top["bytes_per_launch"], "peak_kind": f"of {peak_kind}",
-                     "frac_of_nominal": round(top["gbs"] / NOMINAL_HBM_GBS, 4)},
+                     "frac_of_nominal": round(top["gbs"] / NOMINAL_HBM_GBS, 4),
+                     # DRAM bytes the kernel actually moves per launch (ncu) over its
+                     # event-timed duration: how busy DRAM is, where random reads
+                     # move whole DRAM blocks for narrower rows
+                     "dram_frac": (round(traffic / (top["avg_ms"] * 1e6) / peak, 4) if traffic else None)},
         "kernels": kernels,
         "e2e": e2e,
         "gpu_launches": args.steps * wl.launches_per_step(),
