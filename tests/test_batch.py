@@ -228,6 +228,33 @@ def test_batch_misaligned_arrays(cuda, policy):
 
 
 @pytest.mark.gpu
+def test_batch_runs_of_empty_tasks(cuda):
+    """Long runs of tasks without tiles between real ones (equal tile-prefix
+    values): the kernel's task search must land every tile on its task."""
+    torch = cuda
+    made, made_expect = make_workload(torch, 12, seed=41)
+    pairs = [(t, e) for t, e in zip(made, made_expect) if t["n"] > 0]
+    tasks, want = [], []
+    dummy = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    for k, (t, e) in enumerate(pairs):
+        for _ in range((50, 300, 1, 77, 200)[k % 5]):
+            tasks.append(dict(op=k % 3, width=12, n=0, src=dummy, dst=dummy, idx=None, bound=0))
+        tasks.append(t)
+        want.append((t, e))
+    for _ in range(123):
+        tasks.append(dict(op=0, width=4, n=0, src=dummy, dst=dummy))
+    for tile_bytes in (0, 2048):
+        for t, _ in want:
+            t["dst"].fill_(SENTINEL)
+        b = tg.Batch(tasks, tile_bytes=tile_bytes)
+        b.launch()
+        torch.cuda.synchronize()
+        for t, e in want:
+            assert np.array_equal(t["dst"].cpu().numpy(), e), (t["op"], t["width"], t["n"])
+        b.close()
+
+
+@pytest.mark.gpu
 def test_batch_grid_override_and_empty(cuda):
     torch = cuda
     tasks, expect = make_workload(torch, 40, seed=5)
