@@ -271,7 +271,15 @@ int32_t trv_batch_destroy(trv_batch* batch);
  * (TRV_ERR_UNSUPPORTED beyond).  Every call on a device shares that array and
  * clears its counter on `stream`: calls whose work overlaps on the GPU race
  * and must be ordered by the caller.  The first call on a device looks up the
- * array's address (once per device); make it before any stream capture. */
+ * array's address (once per device); make it before any stream capture.  The
+ * address stays cached for the process: after cudaDeviceReset of a device, do
+ * not call this entry point on that device again.  The plan is copied from
+ * pageable host memory that the call frees on return, so the call may wait
+ * for `stream`'s earlier work before returning, and a stream that is being
+ * captured is refused with TRV_ERR_UNSUPPORTED (trv_batch_capture is the
+ * route for graphs).  A positive opt->grid_blocks is launched as given (above
+ * the device's grid limit: TRV_ERR_CUDA); a current device index of 64 or
+ * more: TRV_ERR_UNSUPPORTED. */
 int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
                              void* stream);
 

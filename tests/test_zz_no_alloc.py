@@ -77,6 +77,54 @@ def test_static_batch_equals_allocating_batch(cuda):
         assert np.array_equal(got, e)
 
 
+def test_static_batch_allocates_nothing(cuda):
+    """Once the kernels are loaded (first call), further calls change neither
+    the device's free memory nor torch's allocator counters."""
+    torch = cuda
+    tasks = workload(torch, 60, seed=23)
+    tg.run_static(tasks)
+    tg.run_static(tasks, blocks_per_sm=2, gather_policy=1, scatter_policy=1)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+    for _ in range(3):
+        tg.run_static(tasks)
+        tg.run_static(tasks, blocks_per_sm=2, gather_policy=1, scatter_policy=1)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert (torch.cuda.memory_allocated(), torch.cuda.memory_reserved()) == (alloc0, reserved0)
+
+
+def test_static_batch_refuses_capture(cuda):
+    """The plan is copied from host memory that lives only for the call, so a
+    capturing stream is refused before anything is enqueued."""
+    torch = cuda
+    src = torch.arange(64, dtype=torch.uint8, device="cuda")
+    dst = torch.zeros_like(src)
+    one = dict(op=0, width=4, n=16, src=src, dst=dst)
+    tg.run_static([one])  # first call (address look-up) outside any capture
+    torch.cuda.synchronize()
+    assert torch.equal(dst, src)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    status = None
+    with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+        try:
+            tg.run_static([one], stream=side)
+        except tg.TroveError as e:
+            status = e.status
+        dst.add_(1)  # keeps the captured graph non-empty
+    assert status == 2  # TRV_ERR_UNSUPPORTED
+    torch.cuda.synchronize()
+    assert torch.equal(dst, src)  # the graph was captured, never replayed
+    dst.zero_()
+    tg.run_static([one], stream=side)  # the stream works normally afterwards
+    side.synchronize()
+    assert torch.equal(dst, src)
+
+
 def test_static_batch_limit(cuda):
     torch = cuda
     src = torch.zeros(64, dtype=torch.uint8, device="cuda")

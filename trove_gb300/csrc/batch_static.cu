@@ -20,7 +20,19 @@
 //    without ordering) race on it and must be serialized by the caller;
 //  - the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (once per device, that device current); make that
-//    first call before any stream capture begins.
+//    first call before any stream capture begins.  The address is cached for
+//    the life of the process: after cudaDeviceReset the device's next
+//    context places the array elsewhere, so a process that resets a device
+//    must not call this entry point on that device again;
+//  - the task table and tile prefix are planned in host memory that lives
+//    only for the duration of the call and are copied to the array with
+//    cudaMemcpyAsync from that pageable memory, which may make the host wait
+//    for the stream's earlier work before the copy starts.  For the same
+//    reason a stream that is being captured is refused (TRV_ERR_UNSUPPORTED):
+//    a captured copy would read the freed host plan on every replay;
+//  - opt->grid_blocks, when positive, is used as the grid as given (a grid
+//    above the device's limit fails the launch with TRV_ERR_CUDA), and a
+//    current device index of 64 or more is refused with TRV_ERR_UNSUPPORTED.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -81,6 +93,11 @@ extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, c
     const int rc = plan_batch(tasks, count, opt, host.data(), prefix.data(), nullptr, &blocks_per_sm);
     if (rc != TRV_OK) return rc;
     if (count == 0 || prefix[count] == 0) return TRV_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &capture);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (capture != cudaStreamCaptureStatusNone) return TRV_ERR_UNSUPPORTED;
     unsigned char* scratch = nullptr;
     const int src = scratch_for_current_device(&scratch);
     if (src != TRV_OK) return src;
@@ -89,8 +106,7 @@ extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, c
     BatchTask* d_tasks = reinterpret_cast<BatchTask*>(scratch);
     long long* d_prefix = reinterpret_cast<long long*>(scratch + kPrefixOffset);
     unsigned long long* d_counter = reinterpret_cast<unsigned long long*>(scratch + kCounterOffset);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemcpyAsync(d_tasks, host.data(), sizeof(BatchTask) * count, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(d_tasks, host.data(), sizeof(BatchTask) * count, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_prefix, prefix.data(), sizeof(long long) * (count + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
