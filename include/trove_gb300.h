@@ -287,6 +287,21 @@ int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, const trv_ba
  * trv_scatter, AUTO path), in order, on `stream`. */
 int32_t trv_run_per_call(const trv_task* tasks, uint64_t count, void* stream);
 
+/* ---- diagnostics -----------------------------------------------------------------
+ * The memory system's ceiling for a random gather, measured on the GPU at hand.
+ * For each i < n, reads every block_bytes-aligned block (32, 64 or 128) of src
+ * that row idx[i] (bytes idx[i]*width .. +width) overlaps, as whole 16-byte
+ * vectors shared by adjacent lanes, with an L2 prefetch-size hint l2_hint
+ * (0 none, 64 or 128 bytes); reads idx sequentially and writes n*width bytes
+ * to dst sequentially (a fold of the blocks, not the rows).  The time of this
+ * call is what a gather of the same rows costs with the best access shape:
+ * the denominator that gathers are compared against.  n % 32 == 0, width a
+ * multiple of 4 up to 128, src aligned to block_bytes and readable up to
+ * src_n*width rounded up to block_bytes, dst 16-byte aligned; indices outside
+ * [0, src_n) read nothing.  No reference counterpart. */
+int32_t trv_probe_block_gather(void* dst, const void* src, uint64_t src_n, const int32_t* idx, uint64_t n,
+                               uint32_t width, uint32_t block_bytes, int32_t l2_hint, void* stream);
+
 /* ---- serving -------------------------------------------------------------------
  * A request loop for copy and gather requests against device-resident sources.
  * Requests are admitted in arrival order while their output fits in the HBM

@@ -81,6 +81,17 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.fill_permutation(bad, 5, 0)) == 3
     assert rc_of(lambda: tg.fill_permutation(ok, 0, 0)) == 0
     assert rc_of(lambda: tg.gather(ok, ok, 10, ok, 5, 12, path="warp", policy=6)) == 1
+    # the random-block probe: n a multiple of 32, 4-byte widths up to 128,
+    # block sizes 32 / 64 / 128, hints none / 64 / 128, block-aligned source
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 0, 12, 64)) == 0
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 48, 12, 64)) == 1
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 64, 14, 64)) == 1
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 64, 132, 64)) == 1
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, 0, 64, 12, 64)) == 1
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 64, 12, 16)) == 2
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok, 64, ok, 64, 12, 64, 32)) == 2
+    assert rc_of(lambda: tg.probe_block_gather(ok, ok + 32, 64, ok, 64, 12, 64)) == 3
+    assert rc_of(lambda: tg.probe_block_gather(ok + 8, ok, 64, ok, 64, 12, 64)) == 3
 
 
 def test_error_carries_status_text(trove_lib):

@@ -127,6 +127,9 @@ _SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "trv_batch_destroy": (ctypes.c_int32, [ctypes.c_void_p]),
     "trv_run_per_call": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.c_void_p]),
+    "trv_probe_block_gather": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                                ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
+                                                ctypes.c_void_p]),
     "trv_batch_run_static": (ctypes.c_int32, [ctypes.POINTER(Task), ctypes.c_uint64, ctypes.POINTER(BatchOptions),
                                               ctypes.c_void_p]),
     "trv_autotune_call": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]),
@@ -254,6 +257,15 @@ def scatter(dst, dst_n: int, src, idx, n: int, width: int, *, path=PATH_AUTO, un
     """dst[idx[i]] = src[i] (trv_scatter_ex); out-of-range indices are skipped."""
     _check(load().trv_scatter_ex(_addr(dst), dst_n, _addr(src), _addr(idx), n, width,
                                  _launch(path, unroll, block, grid, 0, policy), _stream(stream)), "trv_scatter")
+
+
+def probe_block_gather(dst, src, src_n: int, idx, n: int, width: int, block_bytes: int, l2_hint: int = 0, *,
+                       stream=None):
+    """Reads the block_bytes-aligned blocks every row src[idx[i]] overlaps, the
+    indices, and writes n * width bytes (trv_probe_block_gather): the memory
+    system's ceiling for a gather of those rows."""
+    _check(load().trv_probe_block_gather(_addr(dst), _addr(src), src_n, _addr(idx), n, width, block_bytes,
+                                         l2_hint, _stream(stream)), "trv_probe_block_gather")
 
 
 def fill_random_u32(dst, nwords: int, seed: int, *, stream=None):
