@@ -76,6 +76,11 @@ def parse():
     p.add_argument("--workload", choices=["sweep", "copy12", "gather", "batch", "serve", "layout"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--configs", default="copy12,gather,batch,serve",
+                   help="with the sweep (the default workload): the other configs measured after it as "
+                        "sub-records under details.configs, comma-separated, or 'none'")
+    p.add_argument("--sub-cpu-seconds", type=float, default=3.0,
+                   help="CPU-baseline seconds of each sub-record")
     p.add_argument("--no-check", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--array-mib", type=int, default=ARRAY_BYTES >> 20,
@@ -333,6 +338,39 @@ def save_tune_cache(tg, path):
         pass
 
 
+# ---- the reference Trove on the same GPU (a baseline leg) ----------------------
+
+def reference_kernels():
+    """The reference Trove's own kernels for this path, compiled for sm_103a
+    from the reference's headers (the harness cubin the GPU tests also run,
+    built where the reference checkout exists and shipped with the
+    repository).  Returns (module, None) or (None, why)."""
+    try:
+        import oracle
+        ref = oracle.reference_cubin()
+    except Exception as e:  # noqa: BLE001 - reported in the record
+        return None, f"reference cubin not loadable: {e}"
+    if ref is None:
+        return None, "reference cubin not present (built only where the reference checkout exists)"
+    return ref, None
+
+
+def flushed_launch_ms(torch, stream, flush, fn, reps):
+    """Mean CUDA-event time of `reps` launches of fn, each after an L2 flush
+    (outside its events)."""
+    times = []
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        times.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in times) / reps
+
+
 # ---- workloads -------------------------------------------------------------------
 
 class Sweep:
@@ -406,24 +444,53 @@ class Sweep:
         return n * w + self.written[s] * w
 
     def e2e(self, world, steps):
+        """The timed workload itself with host buffers: the same 32 early-exit
+        copies (both APIs, every width, same unrolls) through trv_copy_exit
+        on pinned host arrays, which the copy kernel reads and writes in
+        place over the CPU-GPU link (every byte of input crosses host ->
+        device and every copied byte device -> host inside the timed
+        region)."""
         torch, tg = self.torch, self.tg
         ab = self.array_bytes
-        h_src = torch.empty(ab, dtype=torch.uint8).pin_memory()
-        h_dst = torch.empty(ab, dtype=torch.uint8).pin_memory()
-        h_src.copy_(self.src[:ab].cpu())
-        tg.copy_host(h_dst, h_src, ab // 64, 64)  # warm-up: pins the path and pages the buffers in
+        h_src = torch.empty(ab + 256, dtype=torch.uint8).pin_memory()
+        h_dst = torch.empty(ab + 256, dtype=torch.uint8).pin_memory()
+        h_src.copy_(self.src.cpu())
+        h_dst.fill_(SENTINEL)
+        tg.copy_exit(h_dst, h_src, ab // 64, 64, MODULUS, path=tg.PATH_WARP)  # pages the buffers in
+        torch.cuda.synchronize(self.dev)
+        h_dst.fill_(SENTINEL)
+        stream = torch.cuda.current_stream(self.dev)
         barrier(world)
+        torch.cuda.synchronize(self.dev)
         t0 = time.perf_counter()
         for _ in range(steps):
             for s, w, n in self.plan:
-                tg.copy_host(h_dst, h_src, n, w)
+                for path in (tg.PATH_WARP, tg.PATH_BLOCK):
+                    tg.copy_exit(h_dst, h_src, n, w, MODULUS, path=path, stream=stream)
+        torch.cuda.synchronize(self.dev)
         el = reduce_max(time.perf_counter() - t0, world, self.dev)
-        if not torch.equal(h_dst, h_src):
+        # earlier widths wrote bytes that later widths skip, so check one width
+        # on its own: the widest, both APIs, into a fresh sentinel buffer
+        s, w, n = self.plan[-1]
+        for path in (tg.PATH_WARP, tg.PATH_BLOCK):
+            h_dst.fill_(SENTINEL)
+            tg.copy_exit(h_dst, h_src, n, w, MODULUS, path=path, stream=stream)
+            torch.cuda.synchronize(self.dev)
+            self._check_host_exit(h_dst, h_src, s, w, n)
+        h2d = 2 * sum(n * w for s, w, n in self.plan)
+        d2h = 2 * sum(self.written[s] * w for s, w, n in self.plan)
+        return {"value": round(steps * (h2d + d2h) * world / el / 1e9, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": steps,
+                "path": "the step's 32 early-exit copies through trv_copy_exit (warp and block APIs) on pinned "
+                        "host buffers, read and written in place by the copy kernels over the CPU-GPU link"}
+
+    def _check_host_exit(self, h_dst, h_src, s, w, n):
+        torch = self.torch
+        words0 = h_src[: n * w].view(torch.int32).view(n, s)[:, 0].to(torch.int64) & 0xFFFFFFFF
+        skip = (words0 % MODULUS) == (MODULUS - 1)
+        dv, sv = h_dst[: n * w].view(n, w), h_src[: n * w].view(n, w)
+        if not (torch.equal(dv[~skip], sv[~skip]) and bool((dv[skip] == SENTINEL).all())):
             raise SystemExit("e2e verification failed")
-        io = sum(n * w for s, w, n in self.plan)
-        return {"value": round(steps * 2 * io * world / el / 1e9, 2), "unit": UNIT, "h2d_bytes_per_step": io,
-                "d2h_bytes_per_step": io, "steps": steps,
-                "path": "trv_copy_host per width: pinned host buffers, read and written in place by the copy kernel over the CPU-GPU link"}
 
     def extra(self):
         return {"tuned_unroll": self.tuned}
@@ -457,6 +524,7 @@ class Gather:
         self.flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
         torch.cuda.synchronize(dev)
         self.tuned = {}
+        self.steps = args.steps
 
     def tune(self):
         tg = self.tg
@@ -519,6 +587,122 @@ class Gather:
         return {"value": round(steps * self.bytes_per_step() * world / el / 1e9, 2), "unit": UNIT,
                 "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps, "steps": steps,
                 "path": "per gather: pinned H2D of src + idx, trv_gather, pinned D2H of dst"}
+
+    def reference_gpu(self, kernels):
+        """The reference's coalesced_ptr gather kernel (tests/benchmark.cu:90-99
+        pattern, one struct per thread, 256-thread blocks) and the
+        compiler-generated gather on the same buffers, bit-compared with this
+        library's output and timed the same way (L2 flushed before each
+        launch, mean over as many launches as the timed region had)."""
+        import ctypes
+        torch, tg, n = self.torch, self.tg, GATHER_N
+        ref, why = reference_kernels()
+        if ref is None:
+            return {"unavailable": why}
+        stream = torch.cuda.current_stream(self.dev)
+        out = torch.empty_like(self.dst)
+        own = {k["kernel"]: k for k in kernels}
+        cases, t_ref_sum, t_own_sum, t_dir_sum, alg_sum = [], 0.0, 0.0, 0.0, 0
+        per_pattern = {p: [0.0, 0.0, 0] for p in GATHER_PATTERNS}
+        for w in GATHER_WIDTHS:
+            s = w // 4
+            for p in GATHER_PATTERNS:
+                args = [ctypes.c_void_p(self.idx[p].data_ptr()), ctypes.c_void_p(self.src.data_ptr()),
+                        ctypes.c_void_p(out.data_ptr())]
+
+                def ref_gather():
+                    ref.launch(f"shfl_gather_{s}", n // 256, 256, args, stream.cuda_stream)
+
+                def direct_gather():
+                    ref.launch(f"direct_gather_{s}", n // 256, 256, args, stream.cuda_stream)
+
+                out.zero_()
+                ref_gather()
+                self.dst.zero_()
+                tg.gather(self.dst, self.src, n, self.idx[p], n, w, stream=stream)
+                torch.cuda.synchronize(self.dev)
+                if not torch.equal(out[: n * w], self.dst[: n * w]):
+                    raise SystemExit(f"bench verification failed: reference and library gathers differ ({w} B {p})")
+                t_ref = flushed_launch_ms(torch, stream, self.flush, ref_gather, self.steps)
+                t_dir = flushed_launch_ms(torch, stream, self.flush, direct_gather, 3)
+                key = f"gather_{p}_{w}B"
+                t_own = own[key]["avg_ms"]
+                alg = (2 * w + 4) * n
+                cases.append({"case": key, "reference_gbs": round(alg / t_ref / 1e6, 1),
+                              "this_gbs": round(alg / t_own / 1e6, 1), "ratio": round(t_ref / t_own, 3),
+                              "compiler_gbs": round(alg / t_dir / 1e6, 1)})
+                t_ref_sum += t_ref
+                t_own_sum += t_own
+                t_dir_sum += t_dir
+                alg_sum += alg
+                pp = per_pattern[p]
+                pp[0] += t_ref
+                pp[1] += t_own
+                pp[2] += alg
+        return {"kernel": "shfl_gather_<s> (reference coalesced_ptr gather) and direct_gather_<s> (compiler)",
+                "bit_exact_vs_library": True, "launches_per_case": self.steps,
+                "l2": "flushed before every launch, as this library's",
+                "reference_gbs": round(alg_sum / t_ref_sum / 1e6, 1), "this_gbs": round(alg_sum / t_own_sum / 1e6, 1),
+                "compiler_gbs": round(alg_sum / t_dir_sum / 1e6, 1), "ratio": round(t_ref_sum / t_own_sum, 3),
+                "ratio_by_pattern": {p: round(v[0] / v[1], 3) for p, v in per_pattern.items()},
+                "cases": cases}
+
+    def ceiling(self, kernels, refrec):
+        """Per gather, the memory system's ceiling for its rows
+        (trv_probe_block_gather: every aligned block each row overlaps read
+        whole, best of block sizes 32 / 64 / 128 with each L2 prefetch-size
+        hint, indices read and n * width bytes written), as gather bytes per
+        second, and each implementation's fraction of it.  Plus the plain
+        rate of random reads of aligned 32 / 64 / 128-byte blocks."""
+        torch, tg, n = self.torch, self.tg, GATHER_N
+        stream = torch.cuda.current_stream(self.dev)
+        own = {k["kernel"]: k for k in kernels}
+        refc = {c["case"]: c for c in (refrec or {}).get("cases", [])}
+        variants = [(b, h) for b in (32, 64, 128) for h in (0, 64, 128)]
+        reps = 3
+        cases = []
+        for w in GATHER_WIDTHS:
+            for p in GATHER_PATTERNS:
+                alg = (2 * w + 4) * n
+                best = None
+                for b, h in variants:
+                    def probe():
+                        tg.probe_block_gather(self.dst, self.src, n, self.idx[p], n, w, b, h, stream=stream)
+                    probe()
+                    t = flushed_launch_ms(torch, stream, self.flush, probe, reps)
+                    if best is None or t < best[0]:
+                        best = (t, b, h)
+                key = f"gather_{p}_{w}B"
+                ceil = alg / best[0] / 1e6
+                row = {"case": key, "ceiling_gbs": round(ceil, 1), "block_bytes": best[1], "l2_hint": best[2],
+                       "this_frac": round(own[key]["gbs"] / ceil, 3)}
+                if key in refc:
+                    row["reference_frac"] = round(refc[key]["reference_gbs"] / ceil, 3)
+                cases.append(row)
+        # plain random reads of aligned blocks: rows of exactly one block, a
+        # permutation of the rows, over 1 GiB at most
+        blocks = {}
+        perm_half = torch.empty(n // 2, dtype=torch.int32, device=self.dev)
+        tg.fill_permutation(perm_half, n // 2, 5)
+        for b in (32, 64, 128):
+            rows = n if b * n <= (1 << 30) else n // 2
+            ix = self.idx["perm"] if rows == n else perm_half
+            best = None
+            for h in (0, 64, 128):
+                def probe():
+                    tg.probe_block_gather(self.dst, self.src, rows, ix, rows, b, b, h, stream=stream)
+                probe()
+                t = flushed_launch_ms(torch, stream, self.flush, probe, reps)
+                if best is None or t < best[0]:
+                    best = (t, h)
+            blocks[str(b)] = {"blocks": rows, "source_bytes": rows * b, "l2_hint": best[1],
+                              "blocks_per_us": round(rows / best[0] / 1e3, 1),
+                              "read_gbs": round(rows * b / best[0] / 1e6, 1)}
+        del perm_half
+        fr = [c["this_frac"] for c in cases if c["case"].startswith("gather_perm")]
+        return {"probe": "trv_probe_block_gather", "reps": reps, "l2": "flushed before every launch",
+                "this_frac_perm_min": min(fr), "this_frac_perm_mean": round(sum(fr) / len(fr), 3),
+                "cases": cases, "random_block_reads": blocks}
 
     def extra(self):
         return {"tuned": self.tuned}
@@ -690,6 +874,7 @@ class Copy12:
         self.flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
         self.unroll = 0  # the library's default until tuned
         self.tuned = {}
+        self.steps = args.steps
         torch.cuda.synchronize(dev)
 
     def _launch_ms(self, unroll, reps=7):
@@ -750,6 +935,35 @@ class Copy12:
         return {"value": round(steps * self.bytes_per_step() * world / el / 1e9, 2), "unit": UNIT,
                 "h2d_bytes_per_step": COPY12_N * 12, "d2h_bytes_per_step": COPY12_N * 12, "steps": steps,
                 "path": "trv_copy_host: pinned host buffers read and written in place by the copy kernel"}
+
+    def reference_gpu(self, kernels):
+        """The reference's load/store_warp_contiguous copy (one struct per
+        thread, 4096 blocks of 256; tests/benchmark.cu:52-88 pattern) on the
+        same buffers, bit-compared and timed the same way (L2 flushed before
+        each launch, mean over as many launches as the timed region had)."""
+        import ctypes
+        torch = self.torch
+        ref, why = reference_kernels()
+        if ref is None:
+            return {"unavailable": why}
+        stream = torch.cuda.current_stream(self.dev)
+        out = torch.full_like(self.dst, SENTINEL)
+        args = [ctypes.c_void_p(self.src.data_ptr()), ctypes.c_void_p(out.data_ptr())]
+
+        def ref_copy():
+            ref.launch("shfl_copy_3", COPY12_N // 256, 256, args, stream.cuda_stream)
+
+        ref_copy()
+        torch.cuda.synchronize(self.dev)
+        if not torch.equal(out, self.src):
+            raise SystemExit("bench verification failed: reference 12 B copy")
+        t_ref = flushed_launch_ms(torch, stream, self.flush, ref_copy, self.steps)
+        t_own = kernels[0]["avg_ms"]
+        return {"kernel": "shfl_copy_3 (reference load/store_warp_contiguous)", "bit_exact": True,
+                "launches": self.steps, "l2": "flushed before every launch, as this library's",
+                "reference_us": round(t_ref * 1e3, 2), "this_us": round(t_own * 1e3, 2),
+                "reference_gbs": round(self.bytes_per_step() / t_ref / 1e6, 1),
+                "this_gbs": round(self.bytes_per_step() / t_own / 1e6, 1), "ratio": round(t_ref / t_own, 3)}
 
     def extra(self):
         """L2-resident rate: 100 back-to-back launches replayed from one CUDA
@@ -952,15 +1166,18 @@ WORKLOADS = {"sweep": Sweep, "copy12": Copy12, "gather": Gather, "batch": Batch,
 
 # ---- CPU baseline (the oracle's multithreaded port) ----------------------------
 
-def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = None):
-    """(bytes moved, elapsed s, description) of the CPU form of the workload on
-    a bounded sample; runs `steps` passes if given, else passes until
-    `seconds` of work."""
+def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = None, full: bool = False,
+               warmup: int = 1):
+    """The CPU form of the workload (the oracle's multithreaded port) on a
+    bounded sample: runs `steps` passes if given, else passes until `seconds`
+    of work.  Returns (GB/s of the median pass, GB/s over all passes, passes,
+    description).  `full`: the sweep on its real 2 GiB arrays instead of
+    128 MiB ones."""
     import numpy as np
 
     import oracle
     if workload == "sweep":
-        sample = 128 << 20
+        sample = ARRAY_BYTES if full else 128 << 20
         src = oracle.random_words(sample // 4, 0, threads=threads).view(np.uint8)
         dst = np.zeros_like(src)
 
@@ -972,7 +1189,8 @@ def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = 
                     oracle.run_mt(oracle.OP_COPY_EXIT, dst, src, None, n, w, threads, modulus=MODULUS)
                     done += 2 * n * w
             return done
-        desc = "the sweep on a 128 MiB array per width (both APIs), early-exit copy"
+        desc = (f"the sweep on a {sample >> 20} MiB array per width (both APIs), early-exit copy"
+                + (" (the full workload)" if full else ""))
     elif workload == "layout":
         sample = 128 << 20
         src = oracle.random_words(sample // 4, 7, threads=threads).view(np.uint8)
@@ -1056,47 +1274,50 @@ def cpu_sample(workload: str, threads: int, seconds: float, steps: int | None = 
                 done += 2 * n * w + (4 * n if op else 0)
             return done
         desc = "every 32nd array of the batch (128 arrays), same ops, widths and lengths"
-    one()  # warm caches and page in
-    total, el, passes = 0, 0.0, 0
+    for _ in range(max(1, warmup)):  # warm caches and page in
+        one()
+    total, el, passes, rates, times = 0, 0.0, 0, [], []
     while (steps is not None and passes < steps) or (steps is None and (el < seconds or passes == 0)):
         t0 = time.perf_counter()
-        total += one()
-        el += time.perf_counter() - t0
+        moved = one()
+        dt = time.perf_counter() - t0
+        total += moved
+        el += dt
+        rates.append(moved / dt / 1e9)
+        times.append(dt)
         passes += 1
-    return total, el, f"{passes} passes of {desc}, {threads} threads (oracle port)"
+    return (statistics.median(rates), total / el / 1e9, statistics.median(times),
+            f"{passes} passes of {desc}, {threads} threads (oracle port); value = the median pass")
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the CPU form of the path (the oracle's
+    multithreaded port; the reference itself has no CPU implementation) on
+    the machine's host cores.  For the sweep every step is one pass over the
+    full 2 GiB arrays; value = the median step."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_sample(args.workload, threads, 0, steps=1)
-    total, el, desc = cpu_sample(args.workload, threads, 0, steps=args.steps)
-    value = total / el / 1e9
+    med, mean, med_s, desc = cpu_sample(args.workload, threads, 0, steps=args.steps, warmup=args.warmup,
+                                        full=args.workload == "sweep")
     cfg = WORKLOADS[args.workload].config
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el * 1e3 / args.steps, 3),
+        "impl": "reference", "metric": METRIC, "value": round(med, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(med_s * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded splitmix64 words)", "config": cfg,
-        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(med, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                         "mean_over_passes": round(mean, 2),
                          "sample": desc + "; the reference has no CPU implementation of the path"},
-        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": round(med, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
 
-def run_serve(args, world, rank, local):
-    """The serving workload: one open-loop replay per offered load; the
-    reported value is the bytes of all completed requests over the time from
-    each stream's first submission to its last completion."""
-    import torch
-
-    import trove_gb300 as tg
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    tg.load(build_if_missing=True)
-    load_tune_cache(tg, args.tune_cache)
+def serve_record(torch, tg, dev, args, world, rank):
+    """The serving workload: one open-loop replay per offered load; value =
+    the bytes of all completed requests over the time from each stream's
+    first submission to its last completion."""
+    t_start = time.perf_counter()
     wl = Serve(torch, tg, dev, args)
     if not args.no_check:
         wl.verify()
@@ -1108,39 +1329,44 @@ def run_serve(args, world, rank, local):
     peak, peak_kind = hbm_peak()
     value = total_bytes * world / (ms / 1e3) / 1e9
     top = max(wl.rows, key=lambda r: r["gbs"])
-    cpu = None
-    if rank == 0 and world == 1 and args.cpu_seconds > 0:
-        total, el, desc = cpu_sample("serve", os.cpu_count() or 1, args.cpu_seconds)
-        cpu = {"value": round(total / el / 1e9, 2), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": desc}
-    line = {
+    rec = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": len(SERVE_RATES),
         "warmup": 1, "ms_per_step": round(ms / len(SERVE_RATES), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64 words)",
-        "config": Serve.config, "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak,
-        "peak_kind": peak_kind,
+        "config": Serve.config, "bit_exact": not args.no_check,
+        "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak, "peak_kind": peak_kind,
         "roofline": {"bound": "hbm", "kernel": "batch_kernel (served)", "achieved": top["gbs"], "peak": peak,
                      "unit": "GB/s", "frac": round(top["gbs"] / peak, 4), "traffic": None,
                      "peak_kind": f"of {peak_kind}"},
-        "latency_by_load": wl.rows, "p99_ms": {str(r["offered_per_s"]): r["p99_ms"] for r in wl.rows},
-        "e2e": None, "gpu_launches": int(stats["batches"]), "clocks": clock_info, "cpu_baseline": cpu,
+        "latency_by_load": wl.rows, "p50_ms": {str(r["offered_per_s"]): r["p50_ms"] for r in wl.rows},
+        "p99_ms": {str(r["offered_per_s"]): r["p99_ms"] for r in wl.rows},
+        "e2e": None, "gpu_launches": int(stats["batches"]), "clocks": clock_info,
         "details": {"server": stats},
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    del wl
+    rec["cpu_baseline"] = cpu_record("serve", args, world, rank)
+    rec["wall_s"] = round(time.perf_counter() - t_start, 1)
+    return rec
 
 
-def run_trove(args, world, rank, local):
-    import torch
+def cpu_record(workload, args, world, rank, seconds=None, single=False, full=False):
+    """cpu_baseline of a record (rank 0, one GPU only)."""
+    if rank != 0 or world != 1 or args.cpu_seconds <= 0:
+        return None
+    threads = os.cpu_count() or 1
+    med, mean, _, desc = cpu_sample(workload, threads, args.cpu_seconds if seconds is None else seconds,
+                                    full=full)
+    rec = {"value": round(med, 2), "unit": UNIT, "cores": threads, "kind": "port", "mean_over_passes": round(mean, 2),
+           "sample": desc}
+    if single:
+        med1, _, _, desc1 = cpu_sample(workload, 1, 0, steps=1, warmup=0)
+        rec["single_thread"] = {"value": round(med1, 2), "unit": UNIT, "cores": 1, "sample": desc1}
+    return rec
 
-    import trove_gb300 as tg
-    if args.workload == "serve":
-        return run_serve(args, world, rank, local)
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    tg.load(build_if_missing=True)
-    load_tune_cache(tg, args.tune_cache)
-    wl = WORKLOADS[args.workload](torch, tg, dev, args)
+
+def measure(wl, torch, tg, dev, args, world, rank, e2e=True):
+    """Tune, verify and time one workload; returns its JSON record."""
+    t_start = time.perf_counter()
     if not args.no_tune:
         wl.tune()
         save_tune_cache(tg, args.tune_cache)
@@ -1166,19 +1392,11 @@ def run_trove(args, world, rank, local):
     if isinstance(wl, Batch):
         wl._batch_ms = ms / args.steps
         wl.time_per_call(max(3, args.steps // 3))
-    e2e = wl.e2e(world, args.e2e_steps) if args.e2e_steps > 0 else None
-    cpu = None
-    if rank == 0 and world == 1 and args.cpu_seconds > 0:
-        total, el, desc = cpu_sample(args.workload, os.cpu_count() or 1, args.cpu_seconds)
-        total1, el1, desc1 = cpu_sample(args.workload, 1, 0, steps=1)
-        cpu = {"value": round(total / el / 1e9, 2), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": desc,
-               "single_thread": {"value": round(total1 / el1 / 1e9, 2), "unit": UNIT, "cores": 1, "sample": desc1}}
-    line = {
+    rec = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64 words)",
-        "config": wl.config,
+        "config": wl.config, "bit_exact": not args.no_check,
         "fraction_of_hbm_peak": round(value / world / peak, 4), "peak_gbs": peak, "peak_kind": peak_kind,
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["gbs"], "peak": peak,
                      "unit": "GB/s", "frac": top["frac"], "traffic": traffic,
@@ -1189,12 +1407,62 @@ def run_trove(args, world, rank, local):
                      # move whole DRAM blocks for narrower rows
                      "dram_frac": (round(traffic / (top["avg_ms"] * 1e6) / peak, 4) if traffic else None)},
         "kernels": kernels,
-        "e2e": e2e,
+        "e2e": wl.e2e(world, args.e2e_steps) if e2e and args.e2e_steps > 0 else None,
         "gpu_launches": args.steps * wl.launches_per_step(),
         "clocks": clock_info,
-        "cpu_baseline": cpu,
         "details": wl.extra(),
     }
+    if rank == 0 and hasattr(wl, "reference_gpu"):
+        rec["reference_gpu"] = wl.reference_gpu(kernels)
+    if hasattr(wl, "ceiling"):
+        rec["ceiling"] = wl.ceiling(kernels, rec.get("reference_gpu"))
+    rec["wall_s"] = round(time.perf_counter() - t_start, 1)
+    return rec
+
+
+def free_device(torch, dev):
+    import gc
+    gc.collect()
+    torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()
+
+
+def run_trove(args, world, rank, local):
+    import torch
+
+    import trove_gb300 as tg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    tg.load(build_if_missing=True)
+    load_tune_cache(tg, args.tune_cache)
+    if args.workload == "serve":
+        line = serve_record(torch, tg, dev, args, world, rank)
+    else:
+        wl = WORKLOADS[args.workload](torch, tg, dev, args)
+        line = measure(wl, torch, tg, dev, args, world, rank)
+        del wl
+        free_device(torch, dev)
+        full = args.workload == "sweep" and args.array_mib == ARRAY_BYTES >> 20
+        line["cpu_baseline"] = cpu_record(args.workload, args, world, rank, single=True, full=full)
+    if args.workload == "sweep" and args.configs != "none":
+        # the other configs of the benchmark, each measured the same way in
+        # the same process, as sub-records (the headline stays the sweep)
+        subs = {}
+        sub_args = argparse.Namespace(**vars(args))
+        sub_args.cpu_seconds = min(args.cpu_seconds, args.sub_cpu_seconds)
+        for name in [c for c in args.configs.split(",") if c]:
+            if name == "serve":
+                subs[name] = serve_record(torch, tg, dev, sub_args, world, rank)
+            else:
+                wl = WORKLOADS[name](torch, tg, dev, sub_args)
+                rec = measure(wl, torch, tg, dev, sub_args, world, rank, e2e=False)
+                del wl
+                free_device(torch, dev)
+                rec["cpu_baseline"] = cpu_record(name, sub_args, world, rank)
+                subs[name] = rec
+            free_device(torch, dev)
+        line["details"]["configs"] = subs
+        line["gpu_launches"] += sum(r.get("gpu_launches") or 0 for r in subs.values())
     if rank == 0:
         print(json.dumps(line), flush=True)
 

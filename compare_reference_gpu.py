@@ -1,9 +1,9 @@
 """Side-by-side timing of the reference Trove and this library on one GPU.
 
-Not collected by pytest (no test_ prefix): run it directly on a GB300, after
+Run it directly on a GB300, after
 the library and the harness cubins are built:
 
-    python tests/compare_reference_gpu.py [--out FILE] [--reps N] [--tune]
+    python compare_reference_gpu.py [--out FILE] [--reps N] [--tune]
 
 The reference's kernels come from oracle/_ref/trove_ref_kernels.cubin, which
 compiles oracle/trove_bench_kernels.cu (the reference's own test-kernel
@@ -25,6 +25,11 @@ same buffers:
 * the device-API gather (--part api_gather): the coalesced_ptr gather kernel
   source `shfl_gather_<s>` built against the reference's headers and against
   this repository's, widths 4..64 B, the three index patterns;
+* warps with inactive lanes (--part partial): the coalesced_ptr gather and
+  copy kernels `partial_gather_<s>` / `partial_copy_<s>`, in which a seeded
+  10 / 30 / 50 % of the threads leave before the access, built against both
+  header trees: the reference's 16/8/4/2-lane tile cascade against this
+  library's per-lane handling of partial warps, 2^24 structs;
 * the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
   the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
   library: trv_gather), plus the compiler-generated gather
@@ -43,7 +48,7 @@ import statistics
 import sys
 from pathlib import Path
 
-ROOT = Path(__file__).resolve().parent.parent
+ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 MODULUS = 625
@@ -57,7 +62,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial"], default="all")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
@@ -243,6 +248,50 @@ def main():
                        "ratio": round(t_ref / t_own, 3)}
                 rows.append(row)
                 print(json.dumps(row), flush=True)
+
+    if args.part in ("all", "partial"):
+        own = oracle.own_cubin()
+        n = GATHER_N
+        perm = torch.empty(n, dtype=torch.int32, device=dev)
+        tg.fill_permutation(perm, n, 1)
+        torch.cuda.synchronize(dev)
+        for s in (2, 3, 4, 8, 12, 16):
+            w = 4 * s
+            for pct in (10, 30, 50):
+                for kind in ("gather", "copy"):
+                    ex = [ctypes.c_uint32(pct), ctypes.c_uint32(77)]
+                    if kind == "gather":
+                        a_ref = [ctypes.c_void_p(perm.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                                 ctypes.c_void_p(d_ref.data_ptr()), *ex]
+                        a_own = [ctypes.c_void_p(perm.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                                 ctypes.c_void_p(d_own.data_ptr()), *ex]
+                    else:
+                        a_ref = [ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(d_ref.data_ptr()), *ex]
+                        a_own = [ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(d_own.data_ptr()), *ex]
+                    name = f"partial_{kind}_{s}"
+
+                    def ref_k():
+                        cubin(name, n // 256, *a_ref)
+
+                    def own_k():
+                        own.launch(name, n // 256, 256, a_own, stream.cuda_stream)
+
+                    d_ref[: n * w].zero_()
+                    d_own[: n * w].zero_()
+                    ref_k()
+                    own_k()
+                    torch.cuda.synchronize(dev)
+                    if not torch.equal(d_ref[: n * w], d_own[: n * w]):
+                        raise SystemExit(f"outputs differ: {name} at {pct} %")
+                    # bytes of the active rows (+ their indices for the gather)
+                    active = n * (100 - pct) // 100
+                    alg = active * (2 * w + (4 if kind == "gather" else 0))
+                    t_ref, t_own = timed(ref_k), timed(own_k)
+                    row = {"workload": "partial", "kind": kind, "width": w, "inactive_pct": pct,
+                           "reference_gbs": round(alg / t_ref / 1e6, 1), "this_gbs": round(alg / t_own / 1e6, 1),
+                           "ratio": round(t_ref / t_own, 3)}
+                    rows.append(row)
+                    print(json.dumps(row), flush=True)
 
     tg.check_device()
     if args.out:

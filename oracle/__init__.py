@@ -315,10 +315,14 @@ class Cubin:
                     f"cuLaunchKernel({name})")
 
 
-def own_cubin() -> Cubin:
-    return Cubin(_b.build_own_cubin())
+def own_cubin(tile: int = 32) -> Cubin:
+    """The harness kernels built against this repository's headers at
+    TILE_SIZE `tile`."""
+    return Cubin(_b.build_own_cubin(tile))
 
 
-def reference_cubin() -> Cubin | None:
-    p = _b.build_ref_cubin()
+def reference_cubin(tile: int = 32) -> Cubin | None:
+    """The same kernels built against the reference's headers, or None where
+    that prebuilt cubin is absent."""
+    p = _b.build_ref_cubin(tile)
     return Cubin(p) if p is not None and Path(p).exists() else None

@@ -5,10 +5,13 @@ Outputs (all git-ignored):
   oracle/_build/libtrove_emu.so         g++: emu/api_cases.cpp on this repo's
                                         include/ under the host lane emulator
   oracle/_build/trove_own_kernels.cubin nvcc: trove_bench_kernels.cu on include/
+                                        (TILE_SIZE 32; _t16/_t8/_t4/_t2 for
+                                        the other tile sizes)
   oracle/_ref/libtrove_ref_emu.so       g++: emu/api_cases.cpp on the
                                         reference's headers, in place
   oracle/_ref/trove_ref_kernels.cubin   nvcc: trove_bench_kernels.cu on the
-                                        reference's headers, in place
+                                        reference's headers, in place (and
+                                        _t16/_t8/_t4/_t2)
 The two oracle/_ref outputs need the reference checkout, which exists only
 where the repository is developed; on a GPU machine the prebuilt cubin is
 used as shipped.  The reference's own build system is never run: its headers
@@ -27,7 +30,8 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("TROVE_REFERENCE", "/root/reference"))
+# The reference checkout sits beside this repository unless TROVE_REFERENCE names it.
+REFERENCE = Path(os.environ.get("TROVE_REFERENCE", str(ROOT.parent / "reference")))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 ORACLE_LIB = BUILD / "libaos_oracle.so"
@@ -35,6 +39,12 @@ OWN_EMU = BUILD / "libtrove_emu.so"
 OWN_CUBIN = BUILD / "trove_own_kernels.cubin"
 REF_EMU = REF_OUT / "libtrove_ref_emu.so"
 REF_CUBIN = REF_OUT / "trove_ref_kernels.cubin"
+# TILE_SIZE values of the harness cubins (the reference's tests/Makefile knob)
+TILES = (32, 16, 8, 4, 2)
+
+
+def _tiled(path: Path, tile: int) -> Path:
+    return path if tile == 32 else path.with_name(f"{path.stem}_t{tile}{path.suffix}")
 
 
 def _stale(out: Path, *deps: Path) -> bool:
@@ -100,34 +110,39 @@ def build_ref_emu() -> Path | None:
     return REF_EMU
 
 
-def _cubin(include_dir: Path, out: Path, deps):
+def _cubin(include_dir: Path, out: Path, deps, tile: int, defines=()):
     nvcc = _nvcc()
     if nvcc is None:
         return None
     out.parent.mkdir(parents=True, exist_ok=True)
-    if _stale(out, HERE / "trove_bench_kernels.cu", *deps):
+    if _stale(out, HERE / "trove_bench_kernels.cu", HERE / "build_oracle.py", *deps):
         tmp = out.with_suffix(".tmp")
-        _run([nvcc, "-std=c++17", "-cubin", *ARCH, "-O3", "-lineinfo", f"-I{include_dir}",
-              str(HERE / "trove_bench_kernels.cu"), "-o", str(tmp)])
+        _run([nvcc, "-std=c++17", "-cubin", *ARCH, "-O3", "-lineinfo", f"-DTILE_SIZE={tile}", *defines,
+              f"-I{include_dir}", str(HERE / "trove_bench_kernels.cu"), "-o", str(tmp)])
         os.replace(tmp, out)
     return out
 
 
-def build_own_cubin():
-    return _cubin(ROOT / "include", OWN_CUBIN, [ROOT / "include" / "trove"])
+def build_own_cubin(tile: int = 32):
+    return _cubin(ROOT / "include", _tiled(OWN_CUBIN, tile), [ROOT / "include" / "trove"], tile,
+                  defines=("-DTRV_OWN_TREE",))
 
 
-def build_ref_cubin():
+def build_ref_cubin(tile: int = 32):
+    out = _tiled(REF_CUBIN, tile)
     if not reference_present():
-        return REF_CUBIN if REF_CUBIN.exists() else None
-    return _cubin(REFERENCE, REF_CUBIN, [REFERENCE / "trove"])
+        return out if out.exists() else None
+    return _cubin(REFERENCE, out, [REFERENCE / "trove"], tile)
 
 
 def build(emulators: bool = False):
-    """Build the C oracle and the GPU harness cubins; the host-emulator
-    libraries only when `emulators` (the CPU test suite builds those on
-    demand)."""
-    jobs = [build_oracle_lib, build_own_cubin, build_ref_cubin]
+    """Build the C oracle and the GPU harness cubins (every tile size, both
+    header trees; the reference's only where its checkout exists); the
+    host-emulator libraries only when `emulators` (the CPU test suite builds
+    those on demand)."""
+    jobs = [build_oracle_lib]
+    for t in TILES:
+        jobs += [lambda t=t: build_own_cubin(t), lambda t=t: build_ref_cubin(t)]
     if emulators:
         jobs += [build_own_emu, build_ref_emu]
     with ThreadPoolExecutor(len(jobs)) as ex:
