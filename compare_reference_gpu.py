@@ -30,6 +30,12 @@ same buffers:
   10 / 30 / 50 % of the threads leave before the access, built against both
   header trees: the reference's 16/8/4/2-lane tile cascade against this
   library's per-lane handling of partial warps, 2^24 structs;
+* one launch of each data-movement path (--part paths), for profiling the
+  choice between them under ncu: this library's warp-contiguous transposing
+  copy at 12, 24 and 64 B, its flat vector copy, its TMA bulk copy, its
+  row-form and coalesced_ptr gathers at 12 and 64 B (random permutation),
+  and the reference's shfl_copy and shfl_gather kernels at the same widths,
+  each on arrays of 512 MiB (no timing, no comparison: just the launches);
 * the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
   the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
   library: trv_gather), plus the compiler-generated gather
@@ -62,7 +68,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial", "paths"], default="all")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
@@ -97,6 +103,9 @@ def main():
 
     def cubin(name, grid, *ptrs_and_scalars):
         ref.launch(name, grid, 256, list(ptrs_and_scalars), stream.cuda_stream)
+
+    if args.part == "paths":
+        return launch_paths(torch, tg, ref, dev, stream)
 
     rows = []
     src = torch.empty(SWEEP_BYTES + 256, dtype=torch.uint8, device=dev)
@@ -298,6 +307,37 @@ def main():
         with open(args.out, "w") as f:
             json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "tuned": args.tune, "rows": rows}, f,
                       indent=1)
+
+
+def launch_paths(torch, tg, ref, dev, stream):
+    """One launch of every path on 512 MiB arrays (the profiling workload)."""
+    nbytes = 512 << 20
+    src = torch.empty(nbytes + 256, dtype=torch.uint8, device=dev)
+    tg.fill_random_u32(src, (nbytes + 256) // 4, seed=0)
+    dst = torch.empty_like(src)
+    torch.cuda.synchronize(dev)
+    for w in (12, 24, 64):
+        n = nbytes // w
+        tg.copy(dst, src, n, w, path="warp", stream=stream)
+        ref.launch(f"shfl_copy_{w // 4}", n // 256, 256, [ctypes.c_void_p(src.data_ptr()),
+                                                           ctypes.c_void_p(dst.data_ptr())], stream.cuda_stream)
+    n = nbytes // 12
+    tg.copy(dst, src, n, 12, path="vector", stream=stream)
+    tg.copy(dst, src, n, 12, path="bulk", stream=stream)
+    for w in (12, 64):
+        n = nbytes // w // 256 * 256
+        perm = torch.empty(n, dtype=torch.int32, device=dev)
+        tg.fill_permutation(perm, n, 1)
+        tg.gather(dst, src, n, perm, n, w, path="warp", stream=stream)
+        tg.gather(dst, src, n, perm, n, w, path="coalesced", stream=stream)
+        ref.launch(f"shfl_gather_{w // 4}", n // 256, 256,
+                   [ctypes.c_void_p(perm.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                    ctypes.c_void_p(dst.data_ptr())], stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        del perm
+    torch.cuda.synchronize(dev)
+    tg.check_device()
+    print("paths launched", flush=True)
 
 
 if __name__ == "__main__":
