@@ -1416,6 +1416,11 @@ def measure(wl, torch, tg, dev, args, world, rank, e2e=True):
         rec["reference_gpu"] = wl.reference_gpu(kernels)
     if hasattr(wl, "ceiling"):
         rec["ceiling"] = wl.ceiling(kernels, rec.get("reference_gpu"))
+        # the dominant gather against the memory system's ceiling for its rows
+        top_case = {c["case"]: c for c in rec["ceiling"]["cases"]}.get(top["kernel"])
+        if top_case:
+            rec["roofline"]["random_block_ceiling_gbs"] = top_case["ceiling_gbs"]
+            rec["roofline"]["frac_of_random_block_ceiling"] = top_case["this_frac"]
     rec["wall_s"] = round(time.perf_counter() - t_start, 1)
     return rec
 
