@@ -107,6 +107,16 @@ __global__ void uniform_index_kernel(int* idx, long long n, long long bound, uns
     }
 }
 
+__global__ void iota_index_kernel(int* idx, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) idx[i] = (int)i;
+}
+
+// Gather / scatter shapes within this fraction of the best time on random
+// indices are all fast on random indices; the tie is broken on contiguous
+// indices.
+constexpr float kTieBand = 0.02f;
+
 }  // namespace
 
 int len_bucket(uint64_t n) {
@@ -184,17 +194,17 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     float best = -1.f;
     trv_launch pick{};
     std::vector<float> times(cands.size(), -1.f);
+    auto run_cand = [&](const trv_launch& c) -> int {
+        if (exit_op) return trv_copy_exit_ex(s.dst, s.src, n, width, 625u, &c, stream);
+        if (op == TRV_OP_AOS_TO_SOA) return trv_aos_to_soa_ex(s.dst, s.src, n, width, &c, stream);
+        if (op == TRV_OP_SOA_TO_AOS) return trv_soa_to_aos_ex(s.dst, s.src, n, width, &c, stream);
+        if (op == TRV_OP_COPY) return trv_copy_ex(s.dst, s.src, n, width, &c, stream);
+        if (op == TRV_OP_GATHER) return trv_gather_ex(s.dst, s.src, n, s.idx, n, width, &c, stream);
+        return trv_scatter_ex(s.dst, n, s.src, s.idx, n, width, &c, stream);
+    };
     for (size_t ci = 0; ci < cands.size(); ++ci) {
         const trv_launch& c = cands[ci];
-        auto run = [&]() -> int {
-            if (exit_op) return trv_copy_exit_ex(s.dst, s.src, n, width, 625u, &c, stream);
-            if (op == TRV_OP_AOS_TO_SOA) return trv_aos_to_soa_ex(s.dst, s.src, n, width, &c, stream);
-            if (op == TRV_OP_SOA_TO_AOS) return trv_soa_to_aos_ex(s.dst, s.src, n, width, &c, stream);
-            if (op == TRV_OP_COPY) return trv_copy_ex(s.dst, s.src, n, width, &c, stream);
-            if (op == TRV_OP_GATHER) return trv_gather_ex(s.dst, s.src, n, s.idx, n, width, &c, stream);
-            return trv_scatter_ex(s.dst, n, s.src, s.idx, n, width, &c, stream);
-        };
-        const float ms = time_ms(run, st, flush);
+        const float ms = time_ms([&]() -> int { return run_cand(c); }, st, flush);
         times[ci] = ms;
         if (ms > 0.f && (best < 0.f || ms < best)) {
             best = ms;
@@ -202,21 +212,31 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
         }
     }
     if (best < 0.f) return TRV_ERR_CUDA;
-    // Gathers and scatters are tuned on uniform random indices, where unrolls
-    // of the same path and policy often tie; on runs and contiguous stretches
-    // of indices 2 structs per lane measured best or near best at every width
-    // (1 is slower there, 4-8 slower from 24 bytes up), so within 2 % of the
-    // best an unroll of 2 wins.
+    // Gathers and scatters are tuned on uniform random indices, where shapes
+    // of the same path often tie.  The shapes within kTieBand of the best are
+    // timed again on contiguous indices (idx[i] = i), which random timing
+    // cannot see, and the fastest there wins: runs and consecutive stretches
+    // of indices then get the shape that handles them best, at no measurable
+    // cost on random ones.
     float pick_ms = best;
-    if (op == TRV_OP_GATHER || op == TRV_OP_SCATTER)
-        for (size_t ci = 0; ci < cands.size(); ++ci) {
-            const trv_launch& c = cands[ci];
-            if (times[ci] > 0.f && times[ci] <= best * 1.02f && c.path == pick.path &&
-                c.cache_policy == pick.cache_policy && c.unroll == 2 && pick.unroll != 2) {
-                pick = c;
-                pick_ms = times[ci];
+    if (op == TRV_OP_GATHER || op == TRV_OP_SCATTER) {
+        std::vector<size_t> band;
+        for (size_t ci = 0; ci < cands.size(); ++ci)
+            if (times[ci] > 0.f && times[ci] <= best * (1.f + kTieBand)) band.push_back(ci);
+        if (band.size() > 1) {
+            iota_index_kernel<<<device_info().sm_count * 4, 256, 0, st>>>(s.idx, (long long)n);
+            if (cudaGetLastError() != cudaSuccess) return TRV_ERR_CUDA;
+            float best_c = -1.f;
+            for (size_t ci : band) {
+                const float ms = time_ms([&]() -> int { return run_cand(cands[ci]); }, st, flush);
+                if (ms > 0.f && (best_c < 0.f || ms < best_c)) {
+                    best_c = ms;
+                    pick = cands[ci];
+                    pick_ms = times[ci];
+                }
             }
         }
+    }
     TuneChoice ch;
     ch.path = pick.path;
     ch.unroll = pick.unroll;
