@@ -36,6 +36,11 @@ same buffers:
   row-form and coalesced_ptr gathers at 12 and 64 B (random permutation),
   and the reference's shfl_copy and shfl_gather kernels at the same widths,
   each on arrays of 512 MiB (no timing, no comparison: just the launches);
+* the CPU-GPU link (--part host): copy-engine rates host -> device, device ->
+  host and both at once on 2 GiB pinned buffers, and this library's copy and
+  early-exit copy kernels reading and writing pinned host arrays in place
+  (several paths, unrolls and grids), beside a staged pipeline (H2D, device
+  copy, D2H on three streams); the ceiling of any host-buffer (e2e) figure;
 * the gather: 2^24 structs, widths 8..64 B, a permutation, runs of 32 and
   the identity (reference kernel `shfl_gather_<s>`: coalesced_ptr; this
   library: trv_gather), plus the compiler-generated gather
@@ -68,7 +73,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial", "paths"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial", "paths", "host"], default="all")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
@@ -106,6 +111,8 @@ def main():
 
     if args.part == "paths":
         return launch_paths(torch, tg, ref, dev, stream)
+    if args.part == "host":
+        return host_link(torch, tg, dev, args)
 
     rows = []
     src = torch.empty(SWEEP_BYTES + 256, dtype=torch.uint8, device=dev)
@@ -307,6 +314,88 @@ def main():
         with open(args.out, "w") as f:
             json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "tuned": args.tune, "rows": rows}, f,
                       indent=1)
+
+
+def host_link(torch, tg, dev, args):
+    """Rates of the CPU-GPU link on 2 GiB pinned host buffers (median of
+    `reps` CUDA-event-timed runs; GB/s = bytes read + written)."""
+    nb = 2 << 30
+    h_src = torch.empty(nb + 256, dtype=torch.uint8).pin_memory()
+    h_dst = torch.empty(nb + 256, dtype=torch.uint8).pin_memory()
+    h_src.random_(0, 255)
+    d_a = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
+    d_b = torch.empty_like(d_a)
+    rows = []
+
+    def ev(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        ts = []
+        for _ in range(args.reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize(dev)
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    def row(name, nbytes, fn):
+        r = {"workload": "host", "case": name, "gbs": round(nbytes / ev(fn) / 1e6, 1)}
+        rows.append(r)
+        print(json.dumps(r), flush=True)
+
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_a[:nb].copy_(h_src[:nb], non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_dst[:nb].copy_(d_b[:nb], non_blocking=True)
+        torch.cuda.current_stream(dev).wait_stream(s1)
+        torch.cuda.current_stream(dev).wait_stream(s2)
+
+    row("copy engine host->device", nb, lambda: d_a[:nb].copy_(h_src[:nb], non_blocking=True))
+    row("copy engine device->host", nb, lambda: h_dst[:nb].copy_(d_a[:nb], non_blocking=True))
+    row("copy engines both directions at once", 2 * nb, both)
+    row("copy kernel reading host, writing device", nb, lambda: tg.copy(d_a, h_src, nb // 16, 16, path="vector"))
+    row("copy kernel reading device, writing host", nb, lambda: tg.copy(h_dst, d_a, nb // 16, 16, path="vector"))
+    for path, unrolls in (("vector", (2, 4, 8)), ("bulk", (0,)), ("warp", (1, 2, 4, 8))):
+        for u in unrolls:
+            row(f"in-place host copy, 16 B, {path} path, unroll {u}", 2 * nb,
+                lambda: tg.copy(h_dst, h_src, nb // 16, 16, path=path, unroll=u))
+    for grid in (152, 608, 2432):
+        row(f"in-place host copy, 16 B, vector path, {grid} blocks", 2 * nb,
+            lambda: tg.copy(h_dst, h_src, nb // 16, 16, path="vector", grid=grid))
+    for w in (12, 64):
+        n = nb // w
+        for api in ("warp", "block"):
+            for u in (1, 2, 4, 8):
+                row(f"in-place host early-exit copy, {w} B, {api} API, unroll {u}", 2 * n * w,
+                    lambda: tg.copy_exit(h_dst, h_src, n, w, MODULUS, path=api, unroll=u))
+
+    def staged(w, chunk):
+        per = chunk // w
+        n_total = nb // w
+        streams = [torch.cuda.Stream(dev) for _ in range(3)]
+        for k, start in enumerate(range(0, n_total, per)):
+            n = min(per, n_total - start)
+            st, off = streams[k % 3], start * w
+            with torch.cuda.stream(st):
+                d_a[off: off + n * w].copy_(h_src[off: off + n * w], non_blocking=True)
+                tg.copy_exit(d_b[off:], d_a[off:], n, w, MODULUS, path="warp", stream=st)
+                h_dst[off: off + n * w].copy_(d_b[off: off + n * w], non_blocking=True)
+        for st in streams:
+            torch.cuda.current_stream(dev).wait_stream(st)
+
+    for w in (12, 64):
+        for chunk in (16 << 20, 64 << 20, 256 << 20):
+            row(f"staged H2D + device early-exit copy + D2H, {w} B, {chunk >> 20} MiB pieces, 3 streams",
+                2 * nb, lambda: staged(w, chunk))
+    tg.check_device()
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "rows": rows}, f, indent=1)
 
 
 def launch_paths(torch, tg, ref, dev, stream):
