@@ -1,6 +1,14 @@
 #!/usr/bin/env python3
 """Benchmark of the AoS hot path on one GB300 (replicas when N > 1).
 
+With no flags the run covers all five configs of the benchmark: the width
+sweep is the headline (`value`, `roofline`, `e2e`, `cpu_baseline`), and
+copy12, the 21 gathers, the 4096-array batch and the serving stream follow
+as sub-records under `details.configs` (`--configs` picks them, `none` for
+the sweep alone), each with its own clocks, roofline, bit-exact check and
+CPU baseline; copy12 and the gathers also time the reference Trove's own
+kernels on the same buffers, and the gathers their random-block ceiling.
+
 --workload sweep (default; the width sweep): for s = 1..16 uint32 words
   (4..64-byte structs), a 2 GiB array of N_s = 2^31 / (4 s) structs of seeded
   random words is copied through this library's device API twice — once with
@@ -29,9 +37,12 @@ GB/s counts bytes read + bytes written + index bytes.  Every array is far
 larger than L2 or the step streams far more than L2 (129 MB), so no flush is
 needed between iterations (copy12 and gather flush).  Launch shapes come from the library's autotuner,
 run before the timed region (its cache is saved and reloaded).  `e2e` times the
-same work with pinned host buffers in and out inside the timed region.
+same work with pinned host buffers in and out inside the timed region (the
+sweep: its own 32 early-exit copies on pinned host arrays).
 `--impl reference` times the CPU form of the path (the oracle's
-multithreaded port) on a bounded sample of the same workload.
+multithreaded port; the reference has no CPU implementation of its own) on
+the machine's cores: for the sweep one pass over the full 2 GiB arrays per step,
+value = the median step.
 """
 from __future__ import annotations
 
