@@ -409,6 +409,7 @@ class Sweep:
                                l2=self.config["l2"].replace("2 GiB", f"{args.array_mib} MiB"))
         self.written = {s: n for s, _, n in self.plan}
         self.tuned = {}
+        self.steps = args.steps
 
     def tune(self):
         tg = self.tg
@@ -502,6 +503,79 @@ class Sweep:
         dv, sv = h_dst[: n * w].view(n, w), h_src[: n * w].view(n, w)
         if not (torch.equal(dv[~skip], sv[~skip]) and bool((dv[skip] == SENTINEL).all())):
             raise SystemExit("e2e verification failed")
+
+    def reference_gpu(self, kernels):
+        """The reference's own early-exit copy (`exit_copy_<s>`:
+        load_warp_contiguous / store_warp_contiguous with the warp_converged()
+        fallback, one struct per thread, 256-thread blocks) and the
+        compiler-generated AoS copy (`direct_copy_<s>`: r[i] = s[i]) on the
+        same 2 GiB arrays, after checking that the reference writes the same
+        bytes as this library's warp-API kernel; each timed the way the step
+        times this library's kernels (CUDA events around back-to-back
+        launches, inputs far larger than L2, as many launches as the timed
+        region had), against copy_exit_warp_<w>B."""
+        import ctypes
+        torch, tg = self.torch, self.tg
+        ref, why = reference_kernels()
+        if ref is None:
+            return {"unavailable": why}
+        stream = torch.cuda.current_stream(self.dev)
+        out = torch.empty_like(self.dst)
+        own = {k["kernel"]: k for k in kernels}
+
+        def launch_ms(fn, reps):
+            fn()
+            evs = []
+            for _ in range(reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                evs.append((a, b))
+            torch.cuda.synchronize(self.dev)
+            return sum(a.elapsed_time(b) for a, b in evs) / reps
+
+        rows, t_ref_sum, t_own_sum, alg_sum, t_dir_sum, dir_sum = [], 0.0, 0.0, 0, 0.0, 0
+        for s, w, n in self.plan:
+            grid = (n + 255) // 256
+            args = [ctypes.c_void_p(self.src.data_ptr()), ctypes.c_void_p(out.data_ptr()), ctypes.c_longlong(n),
+                    ctypes.c_uint32(MODULUS)]
+            dargs = [ctypes.c_void_p(self.src.data_ptr()), ctypes.c_void_p(out.data_ptr())]
+
+            def ref_exit():
+                ref.launch(f"exit_copy_{s}", grid, 256, args, stream.cuda_stream)
+
+            def ref_direct():  # whole blocks only: that kernel has no bounds check
+                ref.launch(f"direct_copy_{s}", n // 256, 256, dargs, stream.cuda_stream)
+
+            out.fill_(SENTINEL)
+            self.dst.fill_(SENTINEL)
+            ref_exit()
+            tg.copy_exit(self.dst, self.src, n, w, MODULUS, path=tg.PATH_WARP, stream=stream)
+            torch.cuda.synchronize(self.dev)
+            if not torch.equal(out, self.dst):
+                raise SystemExit(f"bench verification failed: reference and library exit copies differ ({w} B)")
+            t_ref = launch_ms(ref_exit, self.steps)
+            t_dir = launch_ms(ref_direct, 3)
+            key = f"copy_exit_warp_{w}B"
+            t_own = own[key]["avg_ms"]
+            alg = self.kernel_bytes(key)
+            dalg = 2 * (n // 256 * 256) * w
+            rows.append({"width": w, "reference_gbs": round(alg / t_ref / 1e6, 1),
+                         "this_gbs": round(alg / t_own / 1e6, 1), "ratio": round(t_ref / t_own, 3),
+                         "compiler_gbs": round(dalg / t_dir / 1e6, 1)})
+            t_ref_sum += t_ref
+            t_own_sum += t_own
+            alg_sum += alg
+            t_dir_sum += t_dir
+            dir_sum += dalg
+        return {"kernel": "exit_copy_<s> (reference load/store_warp_contiguous + warp_converged fallback) and "
+                          "direct_copy_<s> (compiler) vs copy_exit_warp_<w>B",
+                "bit_exact_vs_library": True, "launches_per_width": self.steps,
+                "l2": "inputs larger than L2, back-to-back launches, as this library's",
+                "reference_gbs": round(alg_sum / t_ref_sum / 1e6, 1), "this_gbs": round(alg_sum / t_own_sum / 1e6, 1),
+                "compiler_gbs": round(dir_sum / t_dir_sum / 1e6, 1), "ratio": round(t_ref_sum / t_own_sum, 3),
+                "widths": rows}
 
     def extra(self):
         return {"tuned_unroll": self.tuned}
