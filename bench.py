@@ -1038,17 +1038,23 @@ class Copy12:
         def ref_copy():
             ref.launch("shfl_copy_3", COPY12_N // 256, 256, args, stream.cuda_stream)
 
+        def direct_copy():  # the compiler-generated AoS copy, r[i] = s[i]
+            ref.launch("direct_copy_3", COPY12_N // 256, 256, args, stream.cuda_stream)
+
         ref_copy()
         torch.cuda.synchronize(self.dev)
         if not torch.equal(out, self.src):
             raise SystemExit("bench verification failed: reference 12 B copy")
         t_ref = flushed_launch_ms(torch, stream, self.flush, ref_copy, self.steps)
+        t_dir = flushed_launch_ms(torch, stream, self.flush, direct_copy, self.steps)
         t_own = kernels[0]["avg_ms"]
-        return {"kernel": "shfl_copy_3 (reference load/store_warp_contiguous)", "bit_exact": True,
-                "launches": self.steps, "l2": "flushed before every launch, as this library's",
+        return {"kernel": "shfl_copy_3 (reference load/store_warp_contiguous), direct_copy_3 (compiler)",
+                "bit_exact": True, "launches": self.steps, "l2": "flushed before every launch, as this library's",
                 "reference_us": round(t_ref * 1e3, 2), "this_us": round(t_own * 1e3, 2),
+                "compiler_us": round(t_dir * 1e3, 2),
                 "reference_gbs": round(self.bytes_per_step() / t_ref / 1e6, 1),
-                "this_gbs": round(self.bytes_per_step() / t_own / 1e6, 1), "ratio": round(t_ref / t_own, 3)}
+                "this_gbs": round(self.bytes_per_step() / t_own / 1e6, 1),
+                "compiler_gbs": round(self.bytes_per_step() / t_dir / 1e6, 1), "ratio": round(t_ref / t_own, 3)}
 
     def extra(self):
         """L2-resident rate: 100 back-to-back launches replayed from one CUDA
