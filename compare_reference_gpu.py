@@ -36,6 +36,12 @@ same buffers:
   row-form and coalesced_ptr gathers at 12 and 64 B (random permutation),
   and the reference's shfl_copy and shfl_gather kernels at the same widths,
   each on arrays of 512 MiB (no timing, no comparison: just the launches);
+* one launch each of the random-block probe and of the gathers it bounds
+  (--part probe), for profiling them under ncu: 2^24 structs of 8 and 64 B
+  gathered through a random permutation by trv_probe_block_gather (32-byte
+  blocks for 8 B, 64-byte blocks with the 64-byte hint for 64 B), by
+  trv_gather (the row-form shapes the autotuner picks for them) and by the
+  reference's shfl_gather;
 * the CPU-GPU link (--part host): copy-engine rates host -> device, device ->
   host and both at once on 2 GiB pinned buffers, and this library's copy and
   early-exit copy kernels reading and writing pinned host arrays in place
@@ -73,7 +79,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial", "paths", "host"], default="all")
+    ap.add_argument("--part", choices=["all", "copy12", "sweep", "gather", "api_gather", "partial", "paths", "host", "probe"], default="all")
     ap.add_argument("--tune", action="store_true",
                     help="run the library's autotuner for each width first (launch shapes as tuned)")
     args = ap.parse_args()
@@ -113,6 +119,8 @@ def main():
         return launch_paths(torch, tg, ref, dev, stream)
     if args.part == "host":
         return host_link(torch, tg, dev, args)
+    if args.part == "probe":
+        return launch_probe(torch, tg, ref, dev, stream)
 
     rows = []
     src = torch.empty(SWEEP_BYTES + 256, dtype=torch.uint8, device=dev)
@@ -314,6 +322,28 @@ def main():
         with open(args.out, "w") as f:
             json.dump({"gpu": torch.cuda.get_device_name(dev), "reps": args.reps, "tuned": args.tune, "rows": rows}, f,
                       indent=1)
+
+
+def launch_probe(torch, tg, ref, dev, stream):
+    """One launch each of the probe, trv_gather and the reference's gather on
+    the same 2^24-struct permutation gathers (the profiling workload)."""
+    n = GATHER_N
+    src = torch.empty(n * 64 + 256, dtype=torch.uint8, device=dev)
+    tg.fill_random_u32(src, (n * 64 + 256) // 4, seed=0)
+    dst = torch.empty(n * 64, dtype=torch.uint8, device=dev)
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    tg.fill_permutation(perm, n, 1)
+    # the row-form shapes the autotuner picked for these gathers on this
+    # round's boxes (given explicitly: tuning would add launches to profile)
+    for w, block, hint, policy in ((8, 32, 0, 1), (64, 64, 64, 4)):
+        tg.probe_block_gather(dst, src, n, perm, n, w, block, hint, stream=stream)
+        tg.gather(dst, src, n, perm, n, w, path="warp", unroll=2, policy=policy, stream=stream)
+        ref.launch(f"shfl_gather_{w // 4}", n // 256, 256,
+                   [ctypes.c_void_p(perm.data_ptr()), ctypes.c_void_p(src.data_ptr()),
+                    ctypes.c_void_p(dst.data_ptr())], stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+    tg.check_device()
+    print("probe and gathers launched", flush=True)
 
 
 def host_link(torch, tg, dev, args):
