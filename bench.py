@@ -3,8 +3,9 @@
 
 With no flags the run covers all five configs of the benchmark: the width
 sweep is the headline (`value`, `roofline`, `e2e`, `cpu_baseline`), and
-copy12, the 21 gathers, the 4096-array batch and the serving stream follow
-as sub-records under `details.configs` (`--configs` picks them, `none` for
+copy12, the 21 gathers, the 4096-array batch, the serving stream and the
+AoS <-> SoA conversions follow as sub-records under `details.configs`
+(`--configs` picks them, `none` for
 the sweep alone), each with its own clocks, roofline, bit-exact check and
 CPU baseline; copy12 and the gathers also time the reference Trove's own
 kernels on the same buffers, and the gathers their random-block ceiling.
@@ -87,9 +88,10 @@ def parse():
     p.add_argument("--workload", choices=["sweep", "copy12", "gather", "batch", "serve", "layout"], default="sweep")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--configs", default="copy12,gather,batch,serve",
-                   help="with the sweep (the default workload): the other configs measured after it as "
-                        "sub-records under details.configs, comma-separated, or 'none'")
+    p.add_argument("--configs", default="copy12,gather,batch,serve,layout",
+                   help="with the sweep (the default workload): the other configs (and the AoS<->SoA layout "
+                        "conversions) measured after it as sub-records under details.configs, comma-separated, "
+                        "or 'none'")
     p.add_argument("--sub-cpu-seconds", type=float, default=3.0,
                    help="CPU-baseline seconds of each sub-record")
     p.add_argument("--no-check", action="store_true")
