@@ -1518,6 +1518,29 @@ def measure(wl, torch, tg, dev, args, world, rank, e2e=True):
     return rec
 
 
+def targets(line, subs):
+    """The benchmark's three targets, each with the figure this run measured."""
+    out = {}
+    ks = [k for k in line["kernels"] if k["kernel"].startswith("copy_exit_")]
+    if ks:
+        worst = min(k["gbs"] for k in ks)
+        out["copy_at_85pct_of_hbm_peak_4_64B"] = {
+            "slowest_kernel_gbs": worst, "frac_of_nominal_8000": round(worst / NOMINAL_HBM_GBS, 4),
+            "frac_of_measured": round(worst / line["peak_gbs"], 4), "met": worst >= 0.85 * NOMINAL_HBM_GBS}
+    g = subs.get("gather", {})
+    rg = g.get("reference_gpu", {})
+    if "ratio" in rg:
+        out["random_gather_1p2x_reference"] = {
+            "ratio": rg["ratio"], "ratio_by_pattern": rg.get("ratio_by_pattern"),
+            "frac_of_random_block_ceiling_perm": {k: g["ceiling"][k] for k in ("this_frac_perm_min", "this_frac_perm_mean")}
+            if "ceiling" in g else None,
+            "met": rg.get("ratio_by_pattern", {}).get("perm", 0) >= 1.2}
+    b = subs.get("batch", {}).get("details", {})
+    if "batched_vs_per_call" in b:
+        out["batched_2x_per_call"] = {"ratio": b["batched_vs_per_call"], "met": b["batched_vs_per_call"] >= 2.0}
+    return out
+
+
 def free_device(torch, dev):
     import gc
     gc.collect()
@@ -1561,6 +1584,7 @@ def run_trove(args, world, rank, local):
             free_device(torch, dev)
         line["details"]["configs"] = subs
         line["gpu_launches"] += sum(r.get("gpu_launches") or 0 for r in subs.values())
+        line["details"]["targets"] = targets(line, subs)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
