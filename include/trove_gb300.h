@@ -339,7 +339,9 @@ typedef struct trv_result {
 } trv_result;
 
 typedef struct trv_server_stats {
-    uint64_t submitted, admitted, completed, rejected, batches;
+    uint64_t submitted, admitted, completed, rejected;
+    uint64_t batches;            /* persistent-kernel launches (a batch holding both small and large
+                                    requests is two: the small ones first, completing on their own) */
     uint64_t max_queued;         /* most requests waiting for admission at once */
     uint64_t bytes;              /* algorithmic bytes of completed requests */
     uint64_t budget_in_use;      /* arena bytes held now */

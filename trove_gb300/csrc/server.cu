@@ -7,9 +7,11 @@
 //   2. admission — queued requests, in arrival order, get their output carved
 //      from the budget arena (first fit, 256-byte granules) while it fits;
 //   3. launch — while a batch slot is free, up to max_batch_requests admitted
-//      requests become one batch: its task table and tile prefix are written
+//      requests become one batch: its task table and tile prefixes are written
 //      to the slot's pinned staging, copied to the slot's device table, and
-//      the persistent kernel runs on the slot's stream.
+//      the persistent kernel runs on the slot's stream, once for the batch's
+//      small requests and once for its large ones, each followed by its own
+//      completion event, so small requests do not wait for the largest one.
 // With several slots, batches overlap on the GPU and requests that arrive
 // while others run join the next batch: continuous batching, not a queue in
 // front of a single launch.  Sources and index arrays stay device-resident
@@ -115,6 +117,9 @@ struct Req {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t done_small = nullptr;  // after the small requests' launch, when the batch has two
+    size_t n_small = 0;                // ids[0, n_small) complete at done_small (0: one launch)
+    bool small_done = false;
     BatchTask* d_tasks = nullptr;
     long long* d_prefix = nullptr;
     unsigned long long* d_counter = nullptr;
@@ -127,6 +132,14 @@ struct Slot {
 uint64_t request_bytes(const trv_request& r) {
     return 2 * r.n * r.width + (r.op == TRV_OP_GATHER ? 4 * r.n : 0);
 }
+
+// A batch's requests that move at most this many bytes run in a launch of
+// their own ahead of the larger ones and complete at their own event.  On the
+// serving stream of 50 k requests/s (lengths log-uniform up to 2^23 structs),
+// thresholds of 4 / 16 / 64 / 128 / 256 / 512 MB gave p50 0.161 / 0.154 /
+// 0.155 / 0.159 / 0.176 / 0.193 ms and p99 0.92 / 0.88 / 0.82 / 0.77 / 0.78 /
+// 0.88 ms, against 0.206 / 1.02 ms with one launch per batch.
+constexpr uint64_t kSmallRequestBytes = uint64_t(128) << 20;
 
 }  // namespace
 }  // namespace trv
@@ -157,27 +170,43 @@ struct trv_server {
         return std::chrono::duration<double, std::milli>(clock_type::now() - t0).count();
     }
 
+    void mark_done(uint64_t id, double t) {  // lock held
+        Req& r = reqs[id];
+        r.phase = DONE;
+        r.done_ms = t;
+        ++st.completed;
+        st.bytes += request_bytes(r.r);
+        latencies.push_back(r.done_ms - r.submit_ms);
+        if (cfg.release_when_done && !r.released) {
+            arena.release(r.off, r.bytes);
+            r.released = true;
+        }
+    }
+
     void complete_ready() {  // lock held
         for (Slot& s : slots) {
             if (!s.busy) continue;
+            if (s.n_small && !s.small_done) {
+                const cudaError_t qs = cudaEventQuery(s.done_small);
+                if (qs == cudaSuccess) {
+                    const double t = now_ms();
+                    st.last_done_ms = t;
+                    for (size_t k = 0; k < s.n_small; ++k) mark_done(s.ids[k], t);
+                    s.small_done = true;
+                    finished.notify_all();
+                } else if (qs != cudaErrorNotReady && error == TRV_OK) {
+                    error = cuda_fail(qs);
+                }
+            }
             const cudaError_t q = cudaEventQuery(s.done);
             if (q == cudaErrorNotReady) continue;
             if (q != cudaSuccess && error == TRV_OK) error = cuda_fail(q);
             const double t = now_ms();
             st.last_done_ms = t;
-            for (uint64_t id : s.ids) {
-                Req& r = reqs[id];
-                r.phase = DONE;
-                r.done_ms = t;
-                ++st.completed;
-                st.bytes += request_bytes(r.r);
-                latencies.push_back(r.done_ms - r.submit_ms);
-                if (cfg.release_when_done && !r.released) {
-                    arena.release(r.off, r.bytes);
-                    r.released = true;
-                }
-            }
+            for (size_t k = (s.n_small && s.small_done) ? s.n_small : 0; k < s.ids.size(); ++k) mark_done(s.ids[k], t);
             s.ids.clear();
+            s.n_small = 0;
+            s.small_done = false;
             s.busy = false;
             finished.notify_all();
         }
@@ -197,13 +226,24 @@ struct trv_server {
     }
 
     void launch_ready() {  // lock held
+        const size_t stride = size_t(cfg.max_batch_requests) + 1;  // second prefix array
         for (Slot& s : slots) {
             if (admitted.empty()) return;
             if (s.busy) continue;
             const size_t take = std::min<size_t>(admitted.size(), size_t(cfg.max_batch_requests));
             s.ids.assign(admitted.begin(), admitted.begin() + take);
             admitted.erase(admitted.begin(), admitted.begin() + take);
-            long long tiles = 0;
+            // Small requests run in a launch of their own ahead of the large
+            // ones, with their own completion event: they complete without
+            // waiting for the largest request of the batch.  Each group keeps
+            // its arrival order.
+            const uint64_t small = kSmallRequestBytes;
+            const size_t ns = size_t(std::stable_partition(s.ids.begin(), s.ids.end(),
+                                                           [&](uint64_t id) {
+                                                               return request_bytes(reqs[id].r) <= small;
+                                                           }) -
+                                     s.ids.begin());
+            long long tiles[2] = {0, 0};
             const double t = now_ms();
             for (size_t k = 0; k < take; ++k) {
                 Req& r = reqs[s.ids[k]];
@@ -219,28 +259,46 @@ struct trv_server {
                 p.copy_bulk = 1;
                 const long long nt = plan_task(r.r.op, r.r.width, r.r.n, r.r.src_n, r.r.src, arena.base() + r.off,
                                                r.r.idx, p, &s.h_tasks[k]);
-                s.h_prefix[k] = tiles;
-                tiles += nt;
+                const int grp = k < ns ? 0 : 1;
+                long long* pre = s.h_prefix + (grp ? stride : 0);
+                pre[grp ? k - ns : k] = tiles[grp];
+                tiles[grp] += nt;
                 r.phase = LAUNCHED;
                 r.batch = batches;
                 r.launch_ms = t;
             }
-            s.h_prefix[take] = tiles;
+            s.h_prefix[ns] = tiles[0];
+            s.h_prefix[stride + (take - ns)] = tiles[1];
             cudaError_t e = cudaMemcpyAsync(s.d_tasks, s.h_tasks, sizeof(BatchTask) * take, cudaMemcpyHostToDevice,
                                             s.stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(s.d_prefix, s.h_prefix, sizeof(long long) * (take + 1), cudaMemcpyHostToDevice,
+                e = cudaMemcpyAsync(s.d_prefix, s.h_prefix, sizeof(long long) * (ns + 1), cudaMemcpyHostToDevice,
                                     s.stream);
-            if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), s.stream);
-            if (e == cudaSuccess) {
-                const int g = tiles < grid ? int(tiles > 0 ? tiles : 1) : grid;
-                e = launch_batch_kernel(s.d_tasks, int(take), s.d_prefix, s.d_counter, g, kServerBlocksPerSm, s.stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(s.d_prefix + stride, s.h_prefix + stride, sizeof(long long) * (take - ns + 1),
+                                    cudaMemcpyHostToDevice, s.stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(s.d_counter, 0, 2 * sizeof(unsigned long long), s.stream);
+            const bool two = ns > 0 && ns < take;
+            int launches = 0;
+            if (e == cudaSuccess && ns > 0 && tiles[0] > 0) {
+                const int g = tiles[0] < grid ? int(tiles[0]) : grid;
+                e = launch_batch_kernel(s.d_tasks, int(ns), s.d_prefix, s.d_counter, g, kServerBlocksPerSm, s.stream);
+                ++launches;
+            }
+            if (e == cudaSuccess && two) e = cudaEventRecord(s.done_small, s.stream);
+            if (e == cudaSuccess && ns < take && tiles[1] > 0) {
+                const int g = tiles[1] < grid ? int(tiles[1]) : grid;
+                e = launch_batch_kernel(s.d_tasks + ns, int(take - ns), s.d_prefix + stride, s.d_counter + 1, g,
+                                        kServerBlocksPerSm, s.stream);
+                ++launches;
             }
             if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
             if (e != cudaSuccess && error == TRV_OK) error = cuda_fail(e);
+            s.n_small = two ? ns : 0;
+            s.small_done = false;
             s.busy = true;
             ++batches;
-            ++st.batches;
+            st.batches += uint64_t(launches);
         }
     }
 
@@ -274,6 +332,7 @@ namespace {
 void free_slot(Slot& s) {
     if (s.stream) cudaStreamDestroy(s.stream);
     if (s.done) cudaEventDestroy(s.done);
+    if (s.done_small) cudaEventDestroy(s.done_small);
     if (s.d_tasks) cudaFree(s.d_tasks);
     if (s.d_prefix) cudaFree(s.d_prefix);
     if (s.d_counter) cudaFree(s.d_counter);
@@ -334,11 +393,13 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
     for (Slot& sl : s->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done_small, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_tasks, sizeof(BatchTask) * nt);
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_prefix, sizeof(long long) * (nt + 1));
-        if (e == cudaSuccess) e = cudaMalloc(&sl.d_counter, sizeof(unsigned long long));
+        // two prefix arrays and two work counters: a batch's small and large requests
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_prefix, 2 * sizeof(long long) * (nt + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_counter, 2 * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tasks, sizeof(BatchTask) * nt);
-        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_prefix, sizeof(long long) * (nt + 1));
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_prefix, 2 * sizeof(long long) * (nt + 1));
         if (e != cudaSuccess) {
             cudaGetLastError();
             for (Slot& x : s->slots) free_slot(x);
