@@ -310,7 +310,9 @@ int32_t trv_probe_block_gather(void* dst, const void* src, uint64_t src_n, const
  * `max_inflight` batches run concurrently on separate streams, so requests that
  * arrive while others are on the GPU join the next batch (continuous batching).
  * A dispatcher thread owned by the server does admission, launch and
- * completion.  No reference counterpart. */
+ * completion; while batches are in flight it polls their completion with
+ * yields, keeping one host core busy, and when idle it blocks.  No reference
+ * counterpart. */
 
 typedef struct trv_server_config {
     uint64_t hbm_budget_bytes;   /* output arena size */

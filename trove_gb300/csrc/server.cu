@@ -309,6 +309,12 @@ struct trv_server {
         return false;
     }
 
+    // While batches are in flight the dispatcher polls their events with a
+    // yield between rounds, so it holds one host core busy; idle, it blocks
+    // until a submission or a release wakes it.  A 20-microsecond sleep between
+    // polls (which the kernel's timer slack stretches further) measured p50
+    // 0.094 / 0.165 ms and p99 0.24 / 0.59 ms at 2 k / 50 k requests per
+    // second, against 0.042 / 0.068 ms and 0.16 / 0.42 ms with the yield.
     void run() {
         cudaSetDevice(device);
         std::unique_lock<std::mutex> lk(mu);
@@ -319,7 +325,7 @@ struct trv_server {
             if (stop && queue.empty() && admitted.empty() && !any_busy()) break;
             if (any_busy()) {
                 lk.unlock();
-                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                std::this_thread::yield();
                 lk.lock();
             } else {
                 wake.wait_for(lk, std::chrono::milliseconds(1));
