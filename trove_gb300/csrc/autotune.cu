@@ -260,7 +260,7 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
         const int op = std::get<0>(kv.first);
         // (tile_bytes, blocks per SM, gather / scatter policy, copy tile path)
         std::vector<std::tuple<int, int, int, int>> cands;
-        for (int tb : {64 << 10, 256 << 10, 1 << 20})
+        for (int tb : {32 << 10, 64 << 10, 128 << 10, 256 << 10, 1 << 20})
             for (int bps : {2, 4})
                 for (int gp : {1, 4, 5, 6, 7})
                     for (int cpath : {TRV_PATH_AUTO, TRV_PATH_VECTOR}) {
