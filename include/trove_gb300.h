@@ -226,16 +226,20 @@ typedef struct trv_batch_options {
                             where source and destination are 16-byte aligned) or
                             TRV_PATH_VECTOR (flat vector tiles) */
     int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
-    int32_t blocks_per_sm; /* resident blocks per SM: 4 (64 registers per thread) or 2 (128, for
-                              the register-held gather / scatter rows of policy 1 and 4);
+    int32_t blocks_per_sm; /* resident blocks per SM: 4 (64 registers per thread; every gather and
+                              scatter row staged through shared memory) or 2 (128, which also
+                              offers the register-held rows of policies 1 and 4);
                               0: the autotuned or default choice (4) */
     int32_t gather_policy; /* gather tasks' random loads: 0 the autotuned or default choice (7);
-                              1 plain; 4 with the 64-byte L2 prefetch-size hint; 5 rows staged
-                              through shared memory with asynchronous copies (cp.async); 6 / 7
-                              staged, with the 64 / 128-byte L2 prefetch-size hint */
+                              1 rows held in registers, plain loads; 4 the same with the 64-byte
+                              L2 prefetch-size hint (at 4 blocks per SM, 1 and 4 are staged like
+                              5 and 6); 5 rows staged through shared memory with asynchronous
+                              copies (cp.async); 6 / 7 staged, with the 64 / 128-byte L2
+                              prefetch-size hint */
     int32_t scatter_policy; /* scatter tasks: 0 the autotuned or default choice (5); 1 rows held
-                               in registers; 5 the contiguous source staged through shared
-                               memory with cp.async, stored to the random rows from there */
+                               in registers (at 4 blocks per SM: staged like 5); 5 the contiguous
+                               source staged through shared memory with cp.async, stored to the
+                               random rows from there */
 } trv_batch_options;
 
 typedef struct trv_batch trv_batch;

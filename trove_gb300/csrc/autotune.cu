@@ -271,6 +271,9 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
                         // gathers and scatters; copy groups are timed at the
                         // default budget (4 blocks per SM)
                         if (bps == 2 && op == TRV_OP_COPY) continue;
+                        // the 4-block build stages every row: register-row policies
+                        // would repeat the staged ones there
+                        if (bps == 4 && (gp == 1 || gp == 4) && op != TRV_OP_COPY) continue;
                         cands.push_back({tb, bps, gp, cpath});
                     }
         float best = -1.f;
