@@ -879,17 +879,23 @@ class Batch:
         return self.bytes_per_step()
 
     def time_per_call(self, steps):
+        """The same work as one plain launch per array, each step timed on its
+        own with CUDA events (two warm-up steps first): its host-bound launch
+        loop varies from run to run, so the median step is what is compared."""
         torch = self.torch
         for _ in range(2):
             self.tg.run_per_call(self.tasks, stream=self.stream)
         self.stream.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(self.stream)
+        evs = []
         for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(self.stream)
             self.tg.run_per_call(self.tasks, stream=self.stream)
-        b.record(self.stream)
+            b.record(self.stream)
+            evs.append((a, b))
         self.stream.synchronize()
-        self.per_call_ms = a.elapsed_time(b) / steps
+        self.per_call_steps = sorted(a.elapsed_time(b) for a, b in evs)
+        self.per_call_ms = statistics.median(self.per_call_steps)
 
     def e2e(self, world, steps):
         """Per step: pinned H2D of every source and index array, the batch,
@@ -932,9 +938,12 @@ class Batch:
     def extra(self):
         bps = self.bytes_per_step()
         return {"tiles": self.batch.info()[0], "autotuned": self.tuned,
-                "per_call": {"ms_per_step": round(self.per_call_ms, 3),
+                "per_call": {"ms_per_step": round(self.per_call_ms, 3), "statistic": "median step",
+                             "min_ms": round(self.per_call_steps[0], 3), "max_ms": round(self.per_call_steps[-1], 3),
+                             "steps": len(self.per_call_steps),
                              "value": round(bps / self.per_call_ms / 1e6, 2), "unit": UNIT,
                              "launches_per_step": BATCH_COUNT},
+                "batch_median_ms": round(self._batch_ms, 4),
                 "batched_vs_per_call": round(self.per_call_ms / self._batch_ms, 3)}
 
 
@@ -1483,8 +1492,10 @@ def measure(wl, torch, tg, dev, args, world, rank, e2e=True):
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get(top["kernel"])
     if isinstance(wl, Batch):
-        wl._batch_ms = ms / args.steps
-        wl.time_per_call(max(3, args.steps // 3))
+        # both sides as the median step: the batch's launches from the timed
+        # region, the per-call form's steps timed one by one
+        wl._batch_ms = statistics.median(a.elapsed_time(b) for _, a, b in events)
+        wl.time_per_call(max(5, args.steps // 2))
     rec = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
