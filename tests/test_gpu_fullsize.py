@@ -168,3 +168,75 @@ def test_copy_beyond_2_31_structs(cuda):
     b.close()
     del src, dst
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("width,rows", [(8, 5 << 27), (36, (1 << 27) + 37), (64, (1 << 27) + 37),
+                                        (128, (1 << 26) + 37)])
+def test_index_ops_beyond_4_gib(cuda, width, rows):
+    """Gathers from and scatters into an array of more than 4 GiB, so that most
+    rows' byte offsets need more than 32 bits: every C ABI path, the batch's
+    staged and register movers and the allocation-free batch, against torch's
+    own indexing.  The scatters write distinct rows, each check restores the
+    rows it overwrote, and at the end the whole array must equal a fresh copy
+    of its seeded contents (no row outside the index set was touched)."""
+    torch = cuda
+    n = (1 << 20) + 13
+    big = torch.empty(rows * width, dtype=torch.uint8, device="cuda")
+    tg.fill_random_u32(big, rows * width // 4, seed=width)
+    view = big.view(rows, width)
+    idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    tg.fill_uniform_indices(idx, n, rows, seed=width + 1)
+    assert int((idx.long() * width >= (1 << 32)).sum()) > n // 10
+    expect = view[idx.long()]
+    out = torch.empty(n * width, dtype=torch.uint8, device="cuda")
+    # the struct-typed paths cover widths up to 64 bytes
+    paths = ["auto", "warp", "coalesced", "direct", "vector"] if width <= 64 else ["auto", "warp", "vector"]
+    for path in paths:
+        out.fill_(SENTINEL)
+        tg.gather(out, big, rows, idx, n, width, path=path)
+        torch.cuda.synchronize()
+        assert torch.equal(out.view(n, width), expect), ("gather", path)
+
+    # distinct destination rows spread over the whole array, in random order
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(width)
+    step = (rows - 1) // n
+    didx = (torch.arange(n, device="cuda", dtype=torch.int64) * step + 5)
+    didx = didx[torch.randperm(n, generator=gen, device="cuda")].to(torch.int32)
+    saved = view[didx.long()].clone()
+    payload = torch.empty(n * width, dtype=torch.uint8, device="cuda")
+    tg.fill_random_u32(payload, n * width // 4, seed=width + 2)
+    for path in paths:
+        tg.scatter(big, rows, payload, didx, n, width, path=path)
+        torch.cuda.synchronize()
+        assert torch.equal(view[didx.long()], payload.view(n, width)), ("scatter", path)
+        view[didx.long()] = saved
+
+    if width <= 64:  # the batch's movers serve widths up to 64 bytes
+        for opts in ({}, {"blocks_per_sm": 2, "gather_policy": 1, "scatter_policy": 1}):
+            # one batch each: a gather from the array and a scatter into it
+            # in one batch would race
+            out.fill_(SENTINEL)
+            b = tg.Batch([dict(op=tg.OP_GATHER, width=width, n=n, src=big, dst=out, idx=idx, bound=rows)], **opts)
+            b.launch()
+            torch.cuda.synchronize()
+            b.close()
+            assert torch.equal(out.view(n, width), expect), ("batch gather", opts)
+            b = tg.Batch([dict(op=tg.OP_SCATTER, width=width, n=n, src=payload, dst=big, idx=didx, bound=rows)],
+                         **opts)
+            b.launch()
+            torch.cuda.synchronize()
+            b.close()
+            assert torch.equal(view[didx.long()], payload.view(n, width)), ("batch scatter", opts)
+            view[didx.long()] = saved
+        out.fill_(SENTINEL)
+        tg.run_static([dict(op=tg.OP_GATHER, width=width, n=n, src=big, dst=out, idx=idx, bound=rows)])
+        torch.cuda.synchronize()
+        assert torch.equal(out.view(n, width), expect), "static batch gather"
+
+    fresh = torch.empty_like(big)
+    tg.fill_random_u32(fresh, rows * width // 4, seed=width)
+    assert torch.equal(big, fresh)
+    del big, fresh, view, out, payload, saved, expect
+    torch.cuda.empty_cache()
+    tg.check_device()
