@@ -65,6 +65,10 @@ def test_argument_errors_need_no_gpu(trove_lib):
     assert rc_of(lambda: tg.scatter(ok, 10, ok, ok, 5, 12, path="block")) == 2
     assert rc_of(lambda: tg.copy_exit(ok, ok, 5, 12, 625, path="warp", unroll=5)) == 1
     assert rc_of(lambda: tg.copy(ok, ok, 5, 12, block=128)) == 2
+    # TMA bulk chunks: multiples of 16 whose 4-stage ring fits shared memory
+    assert rc_of(lambda: tg.copy(ok, ok, 5, 12, path="bulk", chunk=24)) == 1
+    assert rc_of(lambda: tg.copy(ok, ok, 5, 12, path="bulk", chunk=64 << 10)) == 1
+    assert rc_of(lambda: tg.copy(ok, ok, 5, 12, path="bulk", chunk=1 << 30)) == 1
     assert rc_of(lambda: tg.fill_random_u32(0, 5, 1)) == 1
     assert rc_of(lambda: tg.copy_host(0, ok, 5, 4)) == 1
     assert rc_of(lambda: tg.aos_to_soa(ok, ok, 5, 68)) == 2

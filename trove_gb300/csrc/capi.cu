@@ -165,7 +165,9 @@ int copy_flat(void* dst, const void* src, uint64_t nbytes, int unroll, int grid_
 int copy_bulk(void* dst, const void* src, uint64_t nbytes, int chunk, int grid_req, cudaStream_t st) {
     if (!bulk_copy_supported(src, dst)) return TRV_ERR_MISALIGNED;
     if (chunk <= 0) chunk = 32 << 10;
-    if (chunk % 16 != 0 || bulk_copy_smem_bytes(chunk) > (227 << 10)) return TRV_ERR_INVALID_ARGUMENT;
+    // chunk is bounded before the ring size is computed, which would overflow
+    if (chunk % 16 != 0 || chunk > (227 << 10) || bulk_copy_smem_bytes(chunk) > (227 << 10))
+        return TRV_ERR_INVALID_ARGUMENT;
     int* flag = device_flag();
     if (!flag) return TRV_ERR_OUT_OF_MEMORY;
     const long long nchunks = (long long)((nbytes + chunk - 1) / chunk);
