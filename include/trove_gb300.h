@@ -320,8 +320,8 @@ int32_t trv_probe_block_gather(void* dst, const void* src, uint64_t src_n, const
 
 typedef struct trv_server_config {
     uint64_t hbm_budget_bytes;   /* output arena size */
-    int32_t max_inflight;        /* concurrent batches (streams); 0: 4 */
-    int32_t max_batch_requests;  /* requests per batch; 0: 1024 */
+    int32_t max_inflight;        /* concurrent batches (streams), at most 64; 0: 4 */
+    int32_t max_batch_requests;  /* requests per batch, at most 65536; 0: 1024 */
     int32_t tile_bytes;          /* 0: autotuner cache, else the size rule */
     int32_t release_when_done;   /* 1: outputs are freed as soon as a request completes */
 } trv_server_config;

@@ -24,8 +24,12 @@ def read_device(ptr, nbytes):
 
 
 def test_server_argument_errors(trove_lib):
-    with pytest.raises(tg.TroveError):
-        tg.Server(0)
+    """Refused before any device work: a zero budget, negative or oversized
+    slot counts and task tables."""
+    for kw in ({}, {"max_inflight": -1}, {"max_inflight": 65}, {"max_batch_requests": (1 << 16) + 1},
+               {"max_batch_requests": (1 << 31) - 1}, {"tile_bytes": -1}):
+        with pytest.raises(tg.TroveError, match="invalid argument"):
+            tg.Server(0 if not kw else 1 << 20, **kw)
 
 
 @pytest.fixture(scope="module")

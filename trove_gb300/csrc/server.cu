@@ -141,6 +141,11 @@ uint64_t request_bytes(const trv_request& r) {
 // 0.88 ms, against 0.206 / 1.02 ms with one launch per batch.
 constexpr uint64_t kSmallRequestBytes = uint64_t(128) << 20;
 
+// Upper limits of the slot count and of a slot's task table (every slot
+// holds a device and a pinned copy of its table).
+constexpr int kMaxInflight = 64;
+constexpr int kMaxBatchRequests = 1 << 16;
+
 }  // namespace
 }  // namespace trv
 
@@ -379,7 +384,8 @@ extern "C" {
 int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
     if (!cfg || !out) return TRV_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_batch_requests < 0 || cfg->tile_bytes < 0)
+    if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_inflight > kMaxInflight ||
+        cfg->max_batch_requests < 0 || cfg->max_batch_requests > kMaxBatchRequests || cfg->tile_bytes < 0)
         return TRV_ERR_INVALID_ARGUMENT;
     // the batch kernel's error flag and set-up, resolved before the dispatcher runs
     if (!device_flag()) return TRV_ERR_CUDA;
