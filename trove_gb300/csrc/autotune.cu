@@ -147,7 +147,7 @@ using namespace trv;
 
 extern "C" {
 
-int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) {
+static int32_t autotune_call_impl(int32_t op, uint32_t width, uint64_t n, void* stream) {
     if (op < TRV_OP_COPY || op > TRV_OP_SOA_TO_AOS || width == 0 || n == 0 || n > (uint64_t(1) << 40) / width)
         return TRV_ERR_INVALID_ARGUMENT;
     const bool exit_op = op == TRV_OP_COPY_EXIT_WARP || op == TRV_OP_COPY_EXIT_BLOCK;
@@ -249,7 +249,11 @@ int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) 
     return TRV_OK;
 }
 
-int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) {
+int32_t trv_autotune_call(int32_t op, uint32_t width, uint64_t n, void* stream) {
+    return no_throw([&] { return autotune_call_impl(op, width, n, stream); });
+}
+
+static int32_t autotune_batch_impl(const trv_task* tasks, uint64_t count, void* stream) {
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const L2Flush flush;
@@ -306,6 +310,10 @@ int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) 
     return TRV_OK;
 }
 
+int32_t trv_autotune_batch(const trv_task* tasks, uint64_t count, void* stream) {
+    return no_throw([&] { return autotune_batch_impl(tasks, count, stream); });
+}
+
 int32_t trv_autotune_lookup(int32_t scope, int32_t op, uint32_t width, uint64_t n, trv_launch* out,
                             int32_t* tile_bytes) {
     TuneChoice c;
@@ -321,7 +329,7 @@ int32_t trv_autotune_clear(void) {
     return TRV_OK;
 }
 
-int32_t trv_autotune_save(const char* path) {
+static int32_t autotune_save_impl(const char* path) {
     if (!path) return TRV_ERR_INVALID_ARGUMENT;
     std::string out = "[\n";
     {
@@ -348,10 +356,14 @@ int32_t trv_autotune_save(const char* path) {
     return ok ? TRV_OK : TRV_ERR_INVALID_ARGUMENT;
 }
 
+int32_t trv_autotune_save(const char* path) {
+    return no_throw([&] { return autotune_save_impl(path); });
+}
+
 // Reads the format trv_autotune_save writes: one object per entry with the
 // integer fields above (gbs may be fractional).  Unknown keys are ignored;
 // entries missing a key field are skipped.
-int32_t trv_autotune_load(const char* path) {
+static int32_t autotune_load_impl(const char* path) {
     if (!path) return TRV_ERR_INVALID_ARGUMENT;
     FILE* f = std::fopen(path, "r");
     if (!f) return TRV_ERR_NOT_FOUND;
@@ -392,6 +404,10 @@ int32_t trv_autotune_load(const char* path) {
         pos = end + 1;
     }
     return loaded > 0 || text.find('[') != std::string::npos ? TRV_OK : TRV_ERR_INVALID_ARGUMENT;
+}
+
+int32_t trv_autotune_load(const char* path) {
+    return no_throw([&] { return autotune_load_impl(path); });
 }
 
 }  // extern "C"

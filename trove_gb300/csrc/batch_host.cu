@@ -166,7 +166,7 @@ using namespace trv;
 
 extern "C" {
 
-int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_options* opt, trv_batch** out) {
+static int32_t batch_create_impl(const trv_task* tasks, uint64_t count, const trv_batch_options* opt, trv_batch** out) {
     if (!out) return TRV_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
@@ -207,6 +207,10 @@ int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_
     if (b->total_tiles < b->grid) b->grid = b->total_tiles > 0 ? int(b->total_tiles) : 1;
     *out = b;
     return TRV_OK;
+}
+
+int32_t trv_batch_create(const trv_task* tasks, uint64_t count, const trv_batch_options* opt, trv_batch** out) {
+    return no_throw([&] { return batch_create_impl(tasks, count, opt, out); });
 }
 
 int32_t trv_batch_launch(trv_batch* b, void* stream) {

@@ -81,7 +81,7 @@ int scratch_for_current_device(unsigned char** out) {
 
 using namespace trv;
 
-extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
+static int32_t batch_run_static_impl(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
                                         void* stream) {
     if (count > 0 && !tasks) return TRV_ERR_INVALID_ARGUMENT;
     if (count > uint64_t(kStaticMaxTasks)) return TRV_ERR_UNSUPPORTED;
@@ -115,4 +115,9 @@ extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, c
     if (prefix[count] < grid) grid = int(prefix[count]);
     e = launch_batch_kernel(d_tasks, int(count), d_prefix, d_counter, grid, blocks_per_sm, st);
     return e == cudaSuccess ? TRV_OK : cuda_fail(e);
+}
+
+extern "C" int32_t trv_batch_run_static(const trv_task* tasks, uint64_t count, const trv_batch_options* opt,
+                                        void* stream) {
+    return no_throw([&] { return batch_run_static_impl(tasks, count, opt, stream); });
 }

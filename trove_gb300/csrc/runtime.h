@@ -5,6 +5,10 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstdint>
+#include <exception>
+
+#include "trove_gb300.h"
 
 namespace trv {
 
@@ -36,6 +40,19 @@ bool one_chunk_per_warp(long long n, int unroll, int requested, int* grid);
 
 int unroll_slot(int unroll);
 int default_unroll(unsigned width);
+
+// Runs an entry point's body so that no C++ exception crosses the C ABI.  The
+// only exceptions the host code can meet are failed allocations of its host
+// containers and of the server's dispatcher thread: both report
+// TRV_ERR_OUT_OF_MEMORY.
+template <typename F>
+int32_t no_throw(F&& body) noexcept {
+    try {
+        return body();
+    } catch (...) {
+        return TRV_ERR_OUT_OF_MEMORY;
+    }
+}
 
 // Records a CUDA error for trv_last_cuda_error() and returns TRV_ERR_CUDA.
 int cuda_fail(cudaError_t e);

@@ -381,7 +381,7 @@ void fill_stats(const std::vector<double>& lat, trv_server_stats* out) {
 
 extern "C" {
 
-int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
+static int32_t server_create_impl(const trv_server_config* cfg, trv_server** out) {
     if (!cfg || !out) return TRV_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 0 || cfg->max_inflight > kMaxInflight ||
@@ -401,7 +401,12 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
         delete s;
         return TRV_ERR_OUT_OF_MEMORY;
     }
-    s->slots.resize(size_t(s->cfg.max_inflight));
+    try {
+        s->slots.resize(size_t(s->cfg.max_inflight));
+    } catch (...) {
+        delete s;
+        return TRV_ERR_OUT_OF_MEMORY;
+    }
     const size_t nt = size_t(s->cfg.max_batch_requests);
     for (Slot& sl : s->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
@@ -429,12 +434,22 @@ int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
     s->grid = std::max(1, resident / s->cfg.max_inflight);
     s->grid_large = std::max(1, resident);
     s->t0 = clock_type::now();
-    s->dispatcher = std::thread([s] { s->run(); });
+    try {
+        s->dispatcher = std::thread([s] { s->run(); });
+    } catch (...) {  // no thread to be had: undo everything above
+        for (Slot& x : s->slots) free_slot(x);
+        delete s;
+        return TRV_ERR_OUT_OF_MEMORY;
+    }
     *out = s;
     return TRV_OK;
 }
 
-int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id) {
+int32_t trv_server_create(const trv_server_config* cfg, trv_server** out) {
+    return no_throw([&] { return server_create_impl(cfg, out); });
+}
+
+static int32_t server_submit_impl(trv_server* s, const trv_request* req, uint64_t* id) {
     if (!s || !req) return TRV_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
     ++s->st.submitted;
@@ -455,6 +470,10 @@ int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id) {
     if (id) *id = k;
     s->wake.notify_one();
     return TRV_OK;
+}
+
+int32_t trv_server_submit(trv_server* s, const trv_request* req, uint64_t* id) {
+    return no_throw([&] { return server_submit_impl(s, req, id); });
 }
 
 static void result_of(trv_server* s, const Req& r, trv_result* out) {
@@ -509,7 +528,7 @@ int32_t trv_server_release(trv_server* s, uint64_t id) {
     return TRV_OK;
 }
 
-int32_t trv_server_stats_get(trv_server* s, trv_server_stats* out) {
+static int32_t server_stats_get_impl(trv_server* s, trv_server_stats* out) {
     if (!s || !out) return TRV_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(s->mu);
     *out = s->st;
@@ -518,7 +537,11 @@ int32_t trv_server_stats_get(trv_server* s, trv_server_stats* out) {
     return s->error;
 }
 
-int32_t trv_server_replay(trv_server* s, const trv_request* reqs, const double* arrival_ms, uint64_t count,
+int32_t trv_server_stats_get(trv_server* s, trv_server_stats* out) {
+    return no_throw([&] { return server_stats_get_impl(s, out); });
+}
+
+static int32_t server_replay_impl(trv_server* s, const trv_request* reqs, const double* arrival_ms, uint64_t count,
                           uint64_t* ids, trv_server_stats* out) {
     if (!s || (count && (!reqs || !arrival_ms))) return TRV_ERR_INVALID_ARGUMENT;
     std::vector<uint64_t> mine(count, 0);
@@ -564,7 +587,12 @@ int32_t trv_server_replay(trv_server* s, const trv_request* reqs, const double* 
     return TRV_OK;
 }
 
-int32_t trv_server_destroy(trv_server* s) {
+int32_t trv_server_replay(trv_server* s, const trv_request* reqs, const double* arrival_ms, uint64_t count,
+                          uint64_t* ids, trv_server_stats* out) {
+    return no_throw([&] { return server_replay_impl(s, reqs, arrival_ms, count, ids, out); });
+}
+
+static int32_t server_destroy_impl(trv_server* s) {
     if (!s) return TRV_ERR_INVALID_ARGUMENT;
     {
         std::lock_guard<std::mutex> g(s->mu);
@@ -579,6 +607,10 @@ int32_t trv_server_destroy(trv_server* s) {
     const int err = s->error;
     delete s;
     return err;
+}
+
+int32_t trv_server_destroy(trv_server* s) {
+    return no_throw([&] { return server_destroy_impl(s); });
 }
 
 }  // extern "C"
