@@ -31,11 +31,27 @@ struct Staging {
     cudaStream_t st[kStages] = {};
 };
 
-Staging& staging_for_device() {
-    static Staging per_device[64];
+constexpr int kMaxDevices = 64;
+
+// The current device's staging, or nullptr past the first kMaxDevices devices.
+Staging* staging_for_device() {
+    static Staging per_device[kMaxDevices];
     int dev = 0;
-    cudaGetDevice(&dev);
-    return per_device[dev >= 0 && dev < 64 ? dev : 0];
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return dev >= 0 && dev < kMaxDevices ? &per_device[dev] : nullptr;
+}
+
+// Waits for every stage's stream, so no copy still reads or writes the
+// caller's buffers once the call returns; the first error wins.
+int drain(Staging& s, int rc) {
+    for (int j = 0; j < kStages; ++j) {
+        const cudaError_t e = cudaStreamSynchronize(s.st[j]);
+        if (e != cudaSuccess && rc == TRV_OK) rc = cuda_fail(e);
+    }
+    return rc;
 }
 
 int prepare(Staging& s) {
@@ -97,7 +113,9 @@ extern "C" int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t 
     if (width == 0 || n > (uint64_t(1) << 62) / width) return TRV_ERR_INVALID_ARGUMENT;
     if (n == 0) return TRV_OK;
     if (!dst_host || !src_host) return TRV_ERR_INVALID_ARGUMENT;
-    Staging& s = staging_for_device();
+    Staging* sp = staging_for_device();
+    if (!sp) return TRV_ERR_UNSUPPORTED;
+    Staging& s = *sp;
     std::lock_guard<std::mutex> guard(s.mu);
     const void* dsrc = nullptr;
     void* ddst = nullptr;
@@ -124,15 +142,11 @@ extern "C" int32_t trv_copy_host(void* dst_host, const void* src_host, uint64_t 
         const uint64_t off = first * width, bytes = cnt * width;
         cudaStream_t st = s.st[k];
         cudaError_t e = cudaMemcpyAsync(s.src[k], in + off, bytes, cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return cuda_fail(e);
+        if (e != cudaSuccess) return drain(s, cuda_fail(e));
         rc = trv_copy(s.dst[k], s.src[k], cnt, width, st);
-        if (rc != TRV_OK) return rc;
+        if (rc != TRV_OK) return drain(s, rc);
         e = cudaMemcpyAsync(out + off, s.dst[k], bytes, cudaMemcpyDeviceToHost, st);
-        if (e != cudaSuccess) return cuda_fail(e);
+        if (e != cudaSuccess) return drain(s, cuda_fail(e));
     }
-    for (int j = 0; j < kStages; ++j) {
-        const cudaError_t e = cudaStreamSynchronize(s.st[j]);
-        if (e != cudaSuccess) return cuda_fail(e);
-    }
-    return TRV_OK;
+    return drain(s, TRV_OK);
 }
