@@ -30,6 +30,10 @@
  *    handle may be used from several (it locks internally).
  *    trv_batch_run_static shares one device array between all callers, so
  *    its calls must not overlap.
+ *  - Devices: the current device of the calling thread.  Batches, servers,
+ *    trv_batch_run_static and the staged form of trv_copy_host serve
+ *    devices 0-63 of the process (others get an error status); the other
+ *    calls serve any device.
  */
 #ifndef TROVE_GB300_H
 #define TROVE_GB300_H

@@ -5,9 +5,9 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <new>
-#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -35,10 +35,17 @@ int check_launch() {
 DeviceInfo& device_info() {
     static std::mutex mu;
     static DeviceInfo infos[64];
+    static std::map<int, DeviceInfo> more;  // devices past the array (map nodes never move)
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) dev = 0;
-    DeviceInfo& d = infos[dev];
+    DeviceInfo* dp;
+    if (dev >= 0 && dev < 64) {
+        dp = &infos[dev];
+    } else {
+        std::lock_guard<std::mutex> g(mu);
+        dp = &more[dev];
+    }
+    DeviceInfo& d = *dp;
     if (!d.ready.load(std::memory_order_acquire)) {
         std::lock_guard<std::mutex> g(mu);
         if (!d.ready.load(std::memory_order_relaxed)) {
@@ -74,13 +81,13 @@ int* device_flag() {
 
 int resident_blocks(const void* func, int block) {
     static std::mutex mu;
-    static std::unordered_map<const void*, int> cache[64];
+    static std::map<std::pair<int, const void*>, int> cache;  // (device, kernel) at 256 threads
     DeviceInfo& d = device_info();
-    const void* key = func;
+    const std::pair<int, const void*> key(d.device, func);
     {
         std::lock_guard<std::mutex> g(mu);
-        auto it = cache[d.device].find(key);
-        if (it != cache[d.device].end() && block == 256) return it->second;
+        auto it = cache.find(key);
+        if (it != cache.end() && block == 256) return it->second;
     }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, block, 0) != cudaSuccess || per_sm < 1)
@@ -88,7 +95,7 @@ int resident_blocks(const void* func, int block) {
     const int r = per_sm * d.sm_count;
     if (block == 256) {
         std::lock_guard<std::mutex> g(mu);
-        cache[d.device][key] = r;
+        cache[key] = r;
     }
     return r;
 }
