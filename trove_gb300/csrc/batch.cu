@@ -392,8 +392,8 @@ __device__ __forceinline__ void tile_staged(const BatchTask& t, long long first,
 }
 
 // Task of tile number `tile`: the last k with prefix[k] <= tile (tasks without
-// tiles repeat a prefix value and are skipped).  Each warp searches on its own,
-// 32 probes per round (3 dependent loads for 4096 tasks instead of 12).
+// tiles repeat a prefix value and are skipped).  One warp searches, 32 probes
+// per round (3 dependent loads for 4096 tasks instead of 12).
 __device__ __forceinline__ int find_task(const long long* __restrict__ prefix, int ntasks, long long tile) {
     const int lane = opaque_tid() & 31;
     int lo = 0, hi = ntasks;  // prefix[lo] <= tile < prefix[hi]
@@ -416,6 +416,8 @@ __global__ void __launch_bounds__(S::block, S::minb)
 batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* __restrict__ tile_prefix,
              unsigned long long* counter, int* flag) {
     __shared__ long long s_tile;
+    __shared__ long long s_begin, s_end;  // tile range of task s_lo
+    __shared__ int s_lo;
     __shared__ __align__(8) unsigned long long s_bar[S::ring];
     extern __shared__ __align__(128) unsigned char s_stage[];  // S::dyn_smem bytes
     int* s_idx = reinterpret_cast<int*>(s_stage + 2 * S::piece);
@@ -423,18 +425,40 @@ batch_kernel(const BatchTask* __restrict__ tasks, int ntasks, const long long* _
     if (threadIdx.x == 0) {
         for (int k = 0; k < S::ring; ++k) mbar_init(&s_bar[k], 1);
         fence_mbarrier_init();
+        s_begin = 0;
+        s_end = 0;  // no task found yet
+        s_lo = 0;
     }
     __syncthreads();
     const long long total = tile_prefix[ntasks];
     for (;;) {
-        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(counter, 1ull);
+        // Warp 0 takes the next tile and, unless it lies in the task of the
+        // block's previous tile, finds its task; the other warps wait at the
+        // barrier and read the result.
+        if (threadIdx.x < 32) {
+            const int lane = opaque_tid() & 31;
+            long long tile = 0;
+            if (lane == 0) tile = (long long)atomicAdd(counter, 1ull);
+            tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
+            if (tile < total && !(tile >= s_begin && tile < s_end)) {
+                const int lo = find_task(tile_prefix, ntasks, tile);
+                __syncwarp();  // every lane has read s_begin / s_end
+                if (lane == 0) {
+                    s_lo = lo;
+                    s_begin = __ldg(tile_prefix + lo);
+                    s_end = __ldg(tile_prefix + lo + 1);
+                }
+            }
+            if (lane == 0) s_tile = tile;
+        }
         __syncthreads();
         const long long tile = s_tile;
-        __syncthreads();
+        const int lo = s_lo;
+        const long long begin = s_begin;
+        __syncthreads();  // read before warp 0 writes the next tile's
         if (tile >= total) break;
-        const int lo = find_task(tile_prefix, ntasks, tile);
         const BatchTask& t = tasks[lo];
-        const long long first = (tile - __ldg(tile_prefix + lo)) * t.tile_structs;
+        const long long first = (tile - begin) * t.tile_structs;
         const long long cnt = t.n - first < t.tile_structs ? t.n - first : t.tile_structs;
         const long long w = 4ll * t.words;
         if (t.op == TRV_OP_COPY) {
