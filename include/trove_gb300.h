@@ -336,7 +336,9 @@ typedef struct trv_request {
     uint64_t n;            /* structs produced */
     const void* src;       /* device source (copy: n structs; gather: src_n structs) */
     uint64_t src_n;        /* gather: source length */
-    const int32_t* idx;    /* gather: n device indices */
+    const int32_t* idx;    /* gather: n device indices; the output struct of an index
+                              outside [0, src_n) is not written, so it holds whatever
+                              the server's arena held there before */
 } trv_request;
 
 typedef struct trv_result {
