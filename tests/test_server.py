@@ -141,3 +141,35 @@ def test_poll_wait_release_cycle(cuda, pools):
     with pytest.raises(tg.TroveError):
         server.release(rid)
     server.close()
+
+
+@pytest.mark.gpu
+def test_gather_with_out_of_range_indices(cuda, pools):
+    """Server gathers skip indices outside [0, src_n): the in-range rows equal
+    the oracle's, and a run of such requests neither faults nor disturbs the
+    requests beside it."""
+    torch = cuda
+    n_pool, src, _, _ = pools
+    rng = np.random.default_rng(11)
+    server = tg.Server(1 << 28, max_inflight=2, max_batch_requests=16)
+    reqs, idx_keep, expect_ok = [], [], []
+    for k, w in enumerate(WIDTHS * 2):
+        n = int(rng.integers(100, 5000))
+        idx_h = rng.integers(0, n_pool, size=n).astype(np.int32)
+        bad = rng.random(n) < 0.2
+        idx_h[bad] = np.where(rng.random(int(bad.sum())) < 0.5, -1 - k, n_pool + k).astype(np.int32)
+        idx = torch.from_numpy(idx_h).cuda()
+        idx_keep.append(idx)
+        reqs.append(dict(op=tg.OP_GATHER, width=w, n=n, src=src[w], src_n=n_pool, idx=idx))
+        src_h = src[w].cpu().numpy().reshape(n_pool, w)
+        expect_ok.append((~bad, src_h[np.where(bad, 0, idx_h)]))
+    torch.cuda.synchronize()
+    ids = [server.submit(r) for r in reqs]
+    for rid, r, (ok, rows) in zip(ids, reqs, expect_ok):
+        res = server.wait(rid)
+        assert res.status == 0
+        got = read_device(res.dst, r["n"] * r["width"]).reshape(r["n"], r["width"])
+        assert np.array_equal(got[ok], rows[ok]), (r["width"], r["n"])
+        server.release(rid)
+    server.close()
+    tg.check_device()
