@@ -229,7 +229,9 @@ typedef struct trv_batch_options {
     int32_t copy_path;   /* copy tasks: TRV_PATH_AUTO (the autotuned choice, else TMA bulk tiles
                             where source and destination are 16-byte aligned) or
                             TRV_PATH_VECTOR (flat vector tiles) */
-    int32_t grid_blocks; /* 0: resident blocks of the persistent kernel */
+    int32_t grid_blocks; /* 0: resident blocks of the persistent kernel; a positive value is
+                            launched as given, capped at the batch's tile count (above the
+                            device's grid limit: TRV_ERR_CUDA at launch) */
     int32_t blocks_per_sm; /* resident blocks per SM: 4 (64 registers per thread; every gather and
                               scatter row staged through shared memory) or 2 (128, which also
                               offers the register-held rows of policies 1 and 4);
