@@ -32,7 +32,8 @@ kernels on the same buffers, and the gathers their random-block ceiling.
   widths uniform from {4,12,20,36,64} B, 50 % copy / 40 % gather (uniform
   indices) / 10 % scatter (permutation); one step = the whole batch as one
   persistent launch replayed from a CUDA graph; the same work as one plain
-  launch per array is timed beside it.
+  launch per array is timed beside it, each of its steps on its own, and
+  `batched_vs_per_call` is its median step over the median batch launch.
 
 GB/s counts bytes read + bytes written + index bytes.  Every array is far
 larger than L2 or the step streams far more than L2 (129 MB), so no flush is
