@@ -68,6 +68,26 @@ def test_batch_argument_errors(trove_lib):
         assert e.value.status == 1
 
 
+def test_static_batch_argument_errors(trove_lib):
+    """trv_batch_run_static validates the tasks and options before touching a
+    device: the same task errors as trv_batch_create, the task limit, and an
+    empty batch is a no-op."""
+    ok = 0x100000
+    for tasks, status in [([dict(op=7, width=12, n=5, src=ok, dst=ok)], 1),
+                          ([dict(op=0, width=13, n=5, src=ok, dst=ok)], 2),
+                          ([dict(op=0, width=12, n=5, src=0, dst=ok)], 1),
+                          ([dict(op=1, width=12, n=5, src=ok + 2, dst=ok, idx=ok, bound=5)], 3),
+                          ([dict(op=0, width=4, n=1, src=ok, dst=ok)] * (tg.STATIC_BATCH_MAX_TASKS + 1), 2)]:
+        with pytest.raises(tg.TroveError) as e:
+            tg.run_static(tasks)
+        assert e.value.status == status
+    with pytest.raises(tg.TroveError) as e:
+        tg.run_static([dict(op=0, width=12, n=5, src=ok, dst=ok)], gather_policy=3)
+    assert e.value.status == 1
+    tg.run_static([])
+    tg.run_static([dict(op=0, width=12, n=0, src=ok, dst=ok)])  # no tiles: nothing to launch
+
+
 def make_workload(torch, count, seed, widths=(4, 12, 20, 36, 64), max_len=20000):
     """Mixed tasks with their expected outputs (oracle)."""
     rng = np.random.default_rng(seed)
