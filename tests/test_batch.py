@@ -45,6 +45,32 @@ def test_autotune_cache_roundtrip(trove_lib, tmp_path):
         tg.autotune_load(tmp_path / "missing.json")
 
 
+def test_autotune_load_rejects_malformed_files(trove_lib, tmp_path):
+    """A cache file is input: an unclosed entry or a file with no entries is
+    refused, an empty array is fine, and a loaded entry whose launch shape is
+    out of range is refused when a call would use it (a TMA chunk of 1 GiB,
+    whose ring size would overflow), before anything reaches a device."""
+    tg.autotune_clear()
+    for text, ok in [('[{"scope": 0, "op": 0', False), ("garbage", False), ("[]", True)]:
+        f = tmp_path / "c.json"
+        f.write_text(text)
+        if ok:
+            tg.autotune_load(f)
+        else:
+            with pytest.raises(tg.TroveError) as e:
+                tg.autotune_load(f)
+            assert e.value.status == 1
+    f = tmp_path / "chunk.json"
+    f.write_text(json.dumps([{"scope": 0, "op": 0, "width": 16, "bucket": 10, "path": 4, "unroll": 0,
+                              "grid": 0, "chunk": 1 << 30, "tile_bytes": 0, "cache_policy": 0}]))
+    tg.autotune_load(f)
+    ok = 0x100000
+    with pytest.raises(tg.TroveError) as e:
+        tg.copy(ok, ok + (64 << 20), 1 << 20, 16)  # AUTO takes the cached TMA shape
+    assert e.value.status == 1
+    tg.autotune_clear()
+
+
 def test_batch_argument_errors(trove_lib):
     ok = 0x100000
     bad_tasks = [
